@@ -1,0 +1,351 @@
+"""Frame-pipeline benchmark: Mtris/s on the 199,712-triangle heightfield at 1280x720.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one frame: Clear + DotGrid + the textured, flat-shaded, clipped
+heightfield (317x317 vertices, heights U[-0.1,0.1], seed 0) at 1280x720.
+Throughput counts submitted faces (Scene.NumTriangles, scene.go:48-54).
+
+value       device-timed: CUDA events around each frame on the library's
+            stream, mesh resident in HBM, L2 flushed (512 MiB write) between
+            frames outside the timed events.
+e2e         the same frames through the public C-ABI call gr_draw with host
+            (page-locked) output buffers: draw items in, RGBA + Z out, copies
+            inside the wall-clock timed region.
+roofline    the kernel with the largest share of frame time, its algorithmic
+            bytes per launch over its CUDA-event duration (profiled pass).
+cpu_baseline the CPU restatement of the reference frame path (the oracle),
+            timed on this host's cores on a bounded number of frames.
+
+--impl reference runs that CPU frame path (all host threads) as the
+reference arm, since the Go reference has no toolchain here.
+N > 1 (torchrun) renders independent replicas of the frame, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "heightfield-199712tris-1280x720-textured-flat-clipped"
+METRIC = "Mtris/s at 1280x720 (plain per-frame)"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def mark(self, begin: bool):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
+
+    def stop(self):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [s for t, s in self.samples if self.t0 and self.t1 and self.t0 - 0.15 <= t <= self.t1 + 0.15]
+        if not rows:
+            rows = [s for _, s in self.samples]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if len(r) > 6 + k and r[6 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(scene):
+    """Bytes a frame must move at minimum (vertices, faces, normals, UVs,
+    texels, RGBA8 + fp32 Z written once), split by the kernel that moves them."""
+    V = sum(o.mesh.nv for o in scene.objects)
+    F = sum(o.mesh.nf for o in scene.objects)
+    flat = bool(scene.flags & 0x10)
+    textured = any(o.mesh.uv is not None for o in scene.objects)
+    project = 16 * V + 12 * F + (16 * F if flat else 0) + (24 * F if textured else 0)
+    texels = sum(4 * t.width * t.height for t in scene.textures if t.pixels is not None)
+    raster = 8 * scene.width * scene.height + texels
+    return {"project": project, "raster": raster, "frame": project + raster}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_ours(args):
+    import gorender_gb300 as gr
+    from gorender_gb300 import _native as N
+    from gorender_gb300 import scenes
+    import ctypes as C
+
+    ws, rank, local = dist_env()
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    scene = scenes.scene_heightfield_1280x720()
+    faces = scene.num_triangles
+    ctx = gr.Context(local)
+    up = gr.UploadedScene(ctx, scene)
+    W, H = scene.width, scene.height
+    npx = W * H
+    L = N.lib()
+    # device outputs owned by the context (NULL pointers)
+    n = len(scene.objects)
+    for _ in range(max(3, args.warmup)):
+        gr.draw_async(ctx, up.items, n, up.params)
+        ctx.flush_l2()
+    ctx.sync()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if pg:
+        pg.barrier()
+    ctx.sync()
+    sampler.mark(True)
+    total_ms = 0.0
+    pairs = 31
+    k = 0
+    while k < args.steps:
+        m = min(pairs, args.steps - k)
+        for j in range(m):
+            ctx.event(2 * j)
+            gr.draw_async(ctx, up.items, n, up.params)
+            ctx.event(2 * j + 1)
+            ctx.flush_l2()
+        for j in range(m):
+            total_ms += ctx.elapsed_ms(2 * j, 2 * j + 1)
+        k += m
+    ctx.sync()
+    sampler.mark(False)
+    launches_per_frame = ctx.last_launches()
+    if pg:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    sampler.stop()
+    ms_per_frame = total_ms / args.steps
+    value = faces * args.steps * ws / (total_ms * 1e-3) / 1e6
+
+    # per-kernel profiled pass (same workload, same stream, events around each kernel)
+    kms = np.zeros(3)
+    kprof = max(20, min(200, args.steps))
+    buf = (C.c_float * 3)()
+    for _ in range(kprof):
+        N.check(L.gr_draw_profiled(ctx.handle, up.items, n, C.byref(up.params), None, None, buf))
+        kms += np.array(buf[:])
+        ctx.flush_l2()
+    kms /= kprof
+    names = ["k_project", "k_bin_big", "k_raster"]
+    top = int(np.argmax(kms))
+    ab = algorithmic_bytes(scene)
+    top_bytes = {0: ab["project"], 1: 0, 2: ab["raster"]}[top]
+    peak, peak_kind = _peaks()
+    achieved = top_bytes / (kms[top] * 1e-3) / 1e9 if kms[top] > 0 else 0.0
+
+    # end to end through gr_draw with page-locked host outputs
+    hp = C.c_void_p()
+    N.check(L.gr_host_alloc(npx * 8, C.byref(hp)))
+    rgba_h = hp.value
+    z_h = hp.value + npx * 4
+    tpf = C.c_int64()
+    e2e_frames = max(10, min(args.steps, 300))
+    for _ in range(3):
+        N.check(L.gr_draw(ctx.handle, up.items, n, C.byref(up.params), rgba_h, z_h, C.byref(tpf)))
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_frames):
+        N.check(L.gr_draw(ctx.handle, up.items, n, C.byref(up.params), rgba_h, z_h, C.byref(tpf)))
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        import torch
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = C.c_int64()
+    d2h = C.c_int64()
+    N.check(L.gr_context_last_transfer_bytes(ctx.handle, C.byref(h2d), C.byref(d2h)))
+    N.check(L.gr_host_free(hp))
+    e2e_value = faces * e2e_frames * ws / e2e_s / 1e6
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(names[top])
+
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mtris/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64",
+        "data": "synthetic (seeded heightfield, seeded 16x16 RGBA8 texture)",
+        "config": {"workload": WORKLOAD, "faces": faces, "width": W, "height": H,
+                   "binned_triangles": int(tpf.value), "parallelism": f"replicas x{ws}",
+                   "l2": "flushed between frames (512 MiB write outside the timed events)"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
+                "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
+                "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
+        "roofline": {"bound": "hbm", "kernel": names[top], "achieved": round(achieved, 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": int(top_bytes),
+                     "kernel_ms": {nm: round(float(v), 5) for nm, v in zip(names, kms)},
+                     "frame_algorithmic_bytes": int(ab["frame"])},
+        "gpu_launches": int(launches_per_frame * args.steps),
+        "clocks": sampler.summary(),
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(scene, args)
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):
+    from oracle import oracle
+    oracle.build()
+    from gorender_gb300 import renderer as R
+    fov = R.fov_radians(scene.fov_deg)
+    mats = [R.object_matrices(o.scale, o.rotation, o.translation, scene.camera.position, scene.camera.direction,
+                              scene.camera.up, scene.width, scene.height, fov) for o in scene.objects]
+    # first frame untimed (builds the ctypes structures, warms caches)
+    oracle.draw_scene(scene, nthreads=nthreads, items_override=mats)
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max_frames and (time.perf_counter() - t_start) < budget_s:
+        t0 = time.perf_counter()
+        _, _, _, st = oracle.draw_scene(scene, nthreads=nthreads, items_override=mats)
+        times.append(time.perf_counter() - t0)
+        assert st == 0
+    return times
+
+
+def cpu_baseline(scene, args):
+    cores = os.cpu_count() or 1
+    nt = min(cores, 64)
+    times = _oracle_frames(scene, nt, budget_s=10.0, max_frames=200)
+    med = statistics.median(times)
+    return {"value": round(scene.num_triangles / med / 1e6, 4), "unit": "Mtris/s", "cores": nt,
+            "kind": "port", "sample": f"{len(times)} full frames of {WORKLOAD}, median frame time "
+            f"{med * 1e3:.2f} ms (C restatement of the reference frame path, objects projected per "
+            f"task, raster in {nt} disjoint row bands)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from gorender_gb300 import scenes
+    scene = scenes.scene_heightfield_1280x720()
+    cores = os.cpu_count() or 1
+    nt = min(cores, 64)
+    from oracle import oracle
+    oracle.build()
+    from gorender_gb300 import renderer as R
+    fov = R.fov_radians(scene.fov_deg)
+    mats = [R.object_matrices(o.scale, o.rotation, o.translation, scene.camera.position, scene.camera.direction,
+                              scene.camera.up, scene.width, scene.height, fov) for o in scene.objects]
+    for _ in range(min(args.warmup, 3)):
+        oracle.draw_scene(scene, nthreads=nt, items_override=mats)
+    # bounded sample: at most ~60 s of frames, at most K frames
+    t0 = time.perf_counter()
+    frames = 0
+    while frames < args.steps and (time.perf_counter() - t0) < 60.0:
+        _, _, _, st = oracle.draw_scene(scene, nthreads=nt, items_override=mats)
+        assert st == 0
+        frames += 1
+    el = time.perf_counter() - t0
+    value = scene.num_triangles * frames / el / 1e6
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mtris/s", "n_gpus": ws,
+        "steps": frames, "warmup": min(args.warmup, 3), "ms_per_step": round(el * 1e3 / frames, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64",
+        "data": "synthetic (seeded heightfield, seeded 16x16 RGBA8 texture)",
+        "config": {"workload": WORKLOAD, "faces": scene.num_triangles, "width": scene.width,
+                   "height": scene.height, "parallelism": "cpu"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mtris/s", "cores": nt, "kind": "port",
+                         "sample": f"{frames} of the requested {args.steps} frames (bounded at 60 s) "
+                                   f"on {nt} threads: C restatement of the reference frame path"},
+        "e2e": {"value": round(value, 4), "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from gorender_gb300 import build as b
+        b.build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

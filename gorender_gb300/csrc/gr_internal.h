@@ -1,0 +1,134 @@
+// gr_internal.h -- structures shared by the host runtime and the sm_103a
+// kernels of the frame pipeline.  Plain C++ (no device code) so both nvcc and
+// the host translation units include it.
+#pragma once
+
+#include <cstdint>
+
+namespace gr {
+
+constexpr int kTileShift = 5;                 // 32 x 32 pixel raster tiles
+constexpr int kTileSize = 1 << kTileShift;
+constexpr int kMaxDim = 16384;                // narrow edge-function bound
+constexpr int kNarrowLimit = 16384;           // |screen coordinate| < 2^14 => int32 edge math
+constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes fans into <= 7
+constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
+constexpr int kProjectThreads = 256;
+constexpr int kRasterThreads = 256;
+constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
+
+// Texture table entry (texture.go:19-26).
+struct DevTex {
+  int kind;             // 0 solid, 1 image (modulo), 2 image fast (mask)
+  int width, height;
+  float widthF, heightF, scale;
+  uint32_t color;       // solid colour, RGBA little-endian
+  const uint32_t* px;   // RGBA8 texels, row-major
+};
+
+// One draw item in device memory: an Object with its matrices.
+struct DevItem {
+  float mvp[16];
+  float world[16];
+  float bbox[32];                   // Mesh.BoundingBox, 8 corners x 4
+  const float* pos;                 // nv x 4
+  const float* vnrm;                // nn x 4
+  const float* fnrm;                // nf x 4
+  const int* vidx;                  // nf x 3
+  const int* nidx;                  // nf x 3 (may be null)
+  const float* uv;                  // nf x 6 (may be null)
+  const int* tex;                   // nf (may be null)
+  const float* vcol;                // nv x 3 (may be null)
+  int nv, nn, nf;
+  uint32_t face_base;               // global face order of face 0
+  int block_base;                   // first project block of this item
+  int pad[3];
+};
+
+// Raster setup of one binned triangle (64 bytes).  For "narrow" triangles
+// (all screen coordinates within +-2^14) the three adjusted edge functions
+// E(x,y) = a*x + b*y + c evaluate exactly in int32 over the screen.
+struct alignas(16) TriRaster {
+  int a01, b01, c01;
+  int a12, b12, c12;
+  int a20, b20, c20;
+  float sumf;                       // float32(E01+E12+E20), constant over the triangle
+  float w0, w1, w2;                 // clip-space W of the vertices (the rasteriser's z)
+  uint32_t key;                     // bit 31: wide; bits 0..30: face*8 + fan + 1
+  int16_t bx0, bx1, by0, by1;       // pixel bounding box clamped to the screen, inclusive
+};
+static_assert(sizeof(TriRaster) == 64, "TriRaster layout");
+
+// int64 edge coefficients of a "wide" triangle (wraparound arithmetic).
+struct alignas(16) TriWide {
+  long long a01, b01, c01, a12, b12, c12, a20, b20, c20;
+  long long pad;
+};
+
+// Shading inputs of one binned triangle (48 bytes).
+struct alignas(16) TriShade {
+  float u0w, v0w, u1w, v1w, u2w, v2w; // u/W and v/W per vertex (rasterizer.go:132-137)
+  float i0, i1, i2;                   // light intensity per vertex
+  int tex;                            // texture slot; -1 = faceColor; -2 = vertex colour
+  float pad[2];
+};
+
+// Per-vertex RGB of a triangle (vertex-colour extension), 3 x 3 floats.
+struct TriColor {
+  float c[9];
+};
+
+// Counters the kernels append to.  Zeroed once at allocation; the raster
+// kernel copies them into DevResult and zeroes them again.
+struct DevWork {
+  unsigned long long tpf;           // binned triangles (Renderer.TPF, one tile)
+  unsigned int nrec;                // raster records written
+  unsigned int nbig;                // records in the multi-tile queue
+  unsigned int bin_need;            // max (bin position + 1) seen when over capacity
+  unsigned int rec_need;            // records needed when over capacity
+  unsigned int big_need;
+  unsigned int error;               // bit 0 clip overflow, bit 1 bad normal index
+};
+
+struct DevResult {
+  unsigned long long tpf;
+  unsigned int nrec, nbig, bin_need, rec_need, big_need, error;
+};
+
+// Everything a frame's kernels need, passed by value.
+struct FrameArgs {
+  int W, H;
+  uint32_t flags;
+  int tiles_x, tiles_y;
+  int num_items;
+  int total_blocks;
+  uint32_t bin_cap;
+  uint32_t rec_cap;
+  uint32_t big_cap;
+  uint32_t key_cap;
+  int vec_ok;                       // outputs allow 16-byte vector stores
+  float S[8];                       // screen matrix rows 0 and 1
+  float L[3];                       // light direction
+  const DevItem* items;
+  const DevTex* texs;
+  int num_tex;
+  TriRaster* rast;
+  TriShade* shade;
+  TriWide* wide;
+  TriColor* tcol;
+  uint32_t* rec_of_key;             // order key -> record index
+  uint32_t* bins;                   // tiles x bin_cap record indices
+  uint32_t* bin_count;              // per tile
+  uint32_t* big;                    // multi-tile record queue
+  DevWork* work;
+  DevResult* result;
+  uint32_t* out_rgba;               // H x W RGBA8
+  float* out_z;                     // H x W
+};
+
+// Kernel launchers (gr_kernels.cu).
+// events (optional): 4 cudaEvent_t recorded before k_project, after k_project,
+// after k_bin_big and after k_raster.
+int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events);
+
+}  // namespace gr

@@ -1,0 +1,207 @@
+/*
+ * gorender_cuda.h -- C-ABI of the GB300 frame pipeline (libgorender_cuda.so).
+ *
+ * This is the boundary a host program binds (cgo, ctypes, JNI ...).  It takes
+ * plain pointers and sizes; no CUDA, C++ or PyTorch type appears here.  Every
+ * entry point returns an int32 status (GR_OK == 0) and never aborts the
+ * process; gr_last_error() gives a message for the calling thread.
+ *
+ * Reference interfaces replaced (file:line in the Go sources):
+ *   NewFrameBuffer (rasterizer.go:15)     -> gr_renderer_create / gr_draw outputs
+ *   NewRenderer + flags (renderer.go:90-148) -> gr_renderer_create/_set_flags/_set_fov
+ *   (*Renderer).Draw (renderer.go:443-483) -> gr_renderer_draw, or gr_draw when
+ *                                             the host builds the matrices itself
+ *   NewMesh / Mesh (mesh.go:20-69)        -> gr_mesh_create
+ *   NewImageTexture / NewColorTexture / SetScale (texture.go:28-67)
+ *                                         -> gr_texture_create
+ *   Renderer.TPF (renderer.go:98, 436-441) -> tpf_out of gr_draw / gr_renderer_tpf
+ *   NewWorldMatrix/NewViewMatrix/NewPerspectiveMatrix/NewScreenMatrix
+ *   (matrix.go:82-118, 133-144)           -> gr_object_matrices / gr_screen_matrix
+ */
+#ifndef GORENDER_CUDA_H
+#define GORENDER_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define GR_OK 0
+#define GR_ERR_INVALID_ARGUMENT 1 /* null pointer, bad size, unknown handle */
+#define GR_ERR_CUDA 2             /* a CUDA runtime call failed */
+#define GR_ERR_OUT_OF_MEMORY 3
+#define GR_ERR_BAD_INDEX 4        /* a face references a missing vertex/normal/texture
+                                     (the reference panics here) */
+#define GR_ERR_BIN_OVERFLOW 5     /* a tile bin overflowed in an asynchronous draw;
+                                     bins have been grown, re-issue the frame */
+#define GR_ERR_CLIP_OVERFLOW 6    /* a clipped polygon exceeded 9 vertices
+                                     (the reference panics here) */
+#define GR_ERR_NO_DEVICE 7
+#define GR_ERR_UNSUPPORTED 8      /* e.g. framebuffer larger than 16384 x 16384 */
+
+/* ---- Renderer flags (renderer.go:90-98); defaults of NewRenderer are
+ *      GR_FLAGS_DEFAULT (renderer.go:130-148). ---- */
+#define GR_FRUSTUM_CLIPPING 0x01u
+#define GR_SHOW_FACES 0x02u
+#define GR_BACKFACE_CULLING 0x04u
+#define GR_LIGHTING 0x08u
+#define GR_FLAT_SHADING 0x10u
+#define GR_SHOW_TEXTURES 0x20u
+#define GR_SHOW_EDGES 0x40u    /* overlay not implemented: rejected with GR_ERR_UNSUPPORTED */
+#define GR_SHOW_VERTICES 0x80u /* overlay not implemented: rejected with GR_ERR_UNSUPPORTED */
+#define GR_FLAGS_DEFAULT (GR_FRUSTUM_CLIPPING | GR_SHOW_FACES | GR_BACKFACE_CULLING | GR_LIGHTING | GR_SHOW_TEXTURES)
+
+/* ---- texture kinds (texture.go:12-17) ---- */
+#define GR_TEXTURE_SOLID 0
+#define GR_TEXTURE_IMAGE 1
+#define GR_TEXTURE_IMAGE_FAST 2 /* power-of-two sizes; chosen by NewImageTexture */
+
+typedef struct gr_context gr_context;
+typedef struct gr_renderer gr_renderer;
+
+/* Thread-local message for the last failing call on this thread. */
+const char* gr_last_error(void);
+/* Library version string. */
+const char* gr_version(void);
+
+/* One context per device and per host thread that draws (Draw is not
+ * reentrant, renderer.go:103-111).  All work runs on a stream the context
+ * owns. */
+int32_t gr_context_create(int32_t device, gr_context** out);
+int32_t gr_context_destroy(gr_context* ctx);
+/* Wait for all queued work; returns the first error an asynchronous draw hit. */
+int32_t gr_context_sync(gr_context* ctx);
+
+/* ---- meshes (mesh.go:20-69), resident in device memory ---- */
+typedef struct {
+  const float* positions;       /* num_vertices x 4 (x, y, z, w=1)  Mesh.Vertices */
+  int32_t num_vertices;
+  const float* vertex_normals;  /* num_normals x 4 (w=1) or NULL    Mesh.VertexNormals */
+  int32_t num_normals;
+  const int32_t* vertex_indices;/* num_faces x 3                     Face.VertexIndices */
+  const int32_t* normal_indices;/* num_faces x 3 or NULL             Face.NormalIndices */
+  const float* uvs;             /* num_faces x 6 or NULL             Face.UVs */
+  const int32_t* face_textures; /* num_faces or NULL; texture handle, -1 = nil  Face.Texture */
+  const float* face_normals;    /* num_faces x 4 or NULL: computed as NewMesh does */
+  const float* vertex_colors;   /* num_vertices x 3 RGB in [0,1] or NULL (extension, no
+                                   counterpart in the reference) */
+  int32_t num_faces;
+} gr_mesh_desc;
+
+/* Uploads a mesh (host pointers).  Vertex indices are checked here; normal
+ * indices are checked when a Gouraud-lit draw first uses them, matching the
+ * reference, which only indexes them there (renderer.go:327-333). */
+int32_t gr_mesh_create(gr_context* ctx, const gr_mesh_desc* desc, int32_t* mesh_out);
+int32_t gr_mesh_destroy(gr_context* ctx, int32_t mesh);
+/* Mesh.BoundingBox as stored at creation (8 x 4 floats). */
+int32_t gr_mesh_bounding_box(gr_context* ctx, int32_t mesh, float* out32);
+
+/* NewImageTexture (kind IMAGE or IMAGE_FAST; rgba = width*height*4 bytes,
+ * already alpha-premultiplied as color.RGBAModel.Convert returns it) or
+ * NewColorTexture (kind SOLID; color = 4 bytes).  scale = Texture.scale. */
+int32_t gr_texture_create(gr_context* ctx, int32_t kind, int32_t width, int32_t height,
+                          const uint8_t* rgba, float scale, const uint8_t* color,
+                          int32_t* texture_out);
+
+/* ---- low-level draw: the host supplies the matrices ---- */
+typedef struct {
+  int32_t mesh;
+  int32_t reserved;
+  float mvp[16];   /* row-major I*P*V*W as projectObject builds it (renderer.go:259-262) */
+  float world[16]; /* row-major NewWorldMatrix (renderer.go:255) */
+} gr_draw_item;
+
+typedef struct {
+  int32_t width, height;  /* framebuffer size, <= 16384 each */
+  uint32_t flags;         /* GR_* renderer flags */
+  int32_t reserved;
+  float screen[16];       /* NewScreenMatrix(width, height) (renderer.go:264) */
+  float light[3];         /* normalised light direction; the reference fixes
+                             Vec3{-1,1,1}.Normalize() (renderer.go:265) */
+} gr_frame_params;
+
+/* Renders one frame: Clear + DotGrid + every item in order (renderer.go:443-483,
+ * sequential order).  rgba_out (width*height*4 bytes, FrameBuffer.Pixels) and
+ * z_out (width*height floats, FrameBuffer.ZBuffer) may be host or device
+ * pointers; either may be NULL.  Blocks until the outputs are complete.
+ * tpf_out (may be NULL) receives the number of binned triangles. */
+int32_t gr_draw(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
+                const gr_frame_params* params, uint8_t* rgba_out, float* z_out,
+                int64_t* tpf_out);
+
+/* Same, enqueued on the context stream without waiting.  Outputs must be
+ * device pointers (or NULL: the context framebuffer).  Errors and bin
+ * overflow surface at the next gr_context_sync. */
+int32_t gr_draw_async(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
+                      const gr_frame_params* params, uint8_t* rgba_dev, float* z_dev);
+
+/* ---- host math (R1: stays on the host, restated from matrix.go) ---- */
+typedef struct {
+  int32_t mesh;
+  float scale[3];        /* Object.Scale */
+  float rotation[3];     /* Object.Rotation, radians */
+  float translation[3];  /* Object.Translation */
+} gr_object;
+
+typedef struct {
+  float position[3];
+  float direction[3];
+  float up[3];
+} gr_camera;
+
+/* (mvp, world) exactly as projectObject computes them for a framebuffer of
+ * width x height, field of view fov_y (radians), zNear 0 and zFar 50. */
+int32_t gr_object_matrices(const gr_object* obj, const gr_camera* cam, int32_t width,
+                           int32_t height, float fov_y, float* mvp_out16, float* world_out16);
+int32_t gr_screen_matrix(int32_t width, int32_t height, float* out16);
+/* Vec3.Normalize (vector.go:78-80). */
+int32_t gr_normalize3(const float* v3, float* out3);
+/* NewMesh face normals (mesh.go:55-60): num_faces x 4 floats. */
+int32_t gr_mesh_face_normals(const float* positions, int32_t num_vertices,
+                             const int32_t* vertex_indices, int32_t num_faces, float* out);
+
+/* ---- high-level Renderer: NewFrameBuffer + NewRenderer + Draw ---- */
+int32_t gr_renderer_create(gr_context* ctx, int32_t width, int32_t height, gr_renderer** out);
+int32_t gr_renderer_destroy(gr_renderer* r);
+int32_t gr_renderer_set_flags(gr_renderer* r, uint32_t flags);
+int32_t gr_renderer_get_flags(gr_renderer* r, uint32_t* flags);
+/* Vertical field of view in radians (NewRenderer uses 45 degrees). */
+int32_t gr_renderer_set_fov(gr_renderer* r, float fov_y);
+int32_t gr_renderer_set_light(gr_renderer* r, const float* direction3);
+/* Renderer.Draw: builds the matrices on the host and renders into the
+ * renderer's device framebuffer. */
+int32_t gr_renderer_draw(gr_renderer* r, const gr_object* objects, int32_t num_objects,
+                         const gr_camera* camera);
+/* Copies FrameBuffer.Pixels / ZBuffer of the last Draw to host or device
+ * memory (either pointer may be NULL). */
+int32_t gr_renderer_read(gr_renderer* r, uint8_t* rgba_out, float* z_out);
+int32_t gr_renderer_tpf(gr_renderer* r, int64_t* tpf);
+
+/* ---- timing helpers (CUDA events on the context stream) ---- */
+int32_t gr_context_event_record(gr_context* ctx, int32_t slot);  /* slot < 64 */
+int32_t gr_context_event_elapsed(gr_context* ctx, int32_t start_slot, int32_t end_slot,
+                                 float* ms);
+/* Writes 'bytes' bytes of a scratch buffer on the context stream (flushes L2
+ * between timed frames). */
+int32_t gr_context_flush_l2(gr_context* ctx, int64_t bytes);
+/* Number of kernels the last frame launched. */
+int32_t gr_context_last_launches(gr_context* ctx, int32_t* launches);
+/* Host<->device bytes the last gr_draw moved (draw items in; result words,
+ * framebuffer and z-buffer out). */
+int32_t gr_context_last_transfer_bytes(gr_context* ctx, int64_t* h2d_bytes, int64_t* d2h_bytes);
+/* gr_draw with CUDA events around each kernel: kernel_ms3 receives the
+ * durations of the project, multi-tile binning and raster kernels.
+ * Synchronous; outputs must be device pointers or NULL. */
+int32_t gr_draw_profiled(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
+                         const gr_frame_params* params, uint8_t* rgba_dev, float* z_dev,
+                         float* kernel_ms3);
+/* Page-locked host memory for framebuffers read back every frame. */
+int32_t gr_host_alloc(int64_t bytes, void** out);
+int32_t gr_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

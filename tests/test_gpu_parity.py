@@ -1,0 +1,138 @@
+"""GPU parity: the CUDA frame pipeline against the CPU oracle, through the C-ABI.
+
+Framebuffer (RGBA8) and z-buffer (float32 bit patterns) must be identical,
+and TPF (binned triangles) must match.  Inputs are seeded synthetic scenes
+small enough for the oracle to finish in seconds.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import gorender_gb300 as gr
+from gorender_gb300 import scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = gr.Context(0)
+    yield c
+    c.close()
+
+
+def compare(ctx, scene, flags=None, light=None):
+    """Render scene on the GPU and with the oracle using the same matrices."""
+    if flags is not None:
+        scene = dataclasses.replace(scene, flags=flags)
+    up = gr.UploadedScene(ctx, scene)
+    if light is not None:
+        up.params = gr.make_params(scene.width, scene.height, scene.flags, light)
+    rgba, z, tpf = up.render()
+    ref_rgba, ref_z, ref_tpf, st = oracle.draw_scene(scene, items_override=up.matrices,
+                                                     light=light, nthreads=4)
+    assert st == 0
+    diff = (rgba != ref_rgba).any(axis=2)
+    zdiff = z.view(np.uint32) != ref_z.view(np.uint32)
+    assert tpf == ref_tpf, f"TPF {tpf} vs oracle {ref_tpf}"
+    assert not diff.any(), f"{int(diff.sum())} RGBA pixels differ, first at {np.argwhere(diff)[:5].tolist()}"
+    assert not zdiff.any(), f"{int(zdiff.sum())} z values differ, first at {np.argwhere(zdiff)[:5].tolist()}"
+    return rgba, z, tpf
+
+
+def test_uvsphere_gouraud(ctx):
+    rgba, z, tpf = compare(ctx, scenes.scene_uvsphere_640x360())
+    assert (z > -1).sum() > 10000
+
+
+@pytest.mark.parametrize("flags", [
+    gr.FLAGS_DEFAULT,
+    gr.FLAGS_DEFAULT & ~gr.BACKFACE_CULLING,
+    gr.FLAGS_DEFAULT & ~gr.LIGHTING,
+    gr.FLAGS_DEFAULT | gr.FLAT_SHADING,
+    gr.FLAGS_DEFAULT & ~gr.FRUSTUM_CLIPPING,
+    gr.FLAGS_DEFAULT & ~gr.SHOW_FACES,
+])
+def test_uvsphere_flags(ctx, flags):
+    sc = scenes.scene_uvsphere_640x360()
+    compare(ctx, sc, flags=flags)
+
+
+def test_heightfield_textured_clipped(ctx):
+    rgba, z, tpf = compare(ctx, scenes.scene_heightfield_1280x720())
+    assert (z > -1).sum() > 100000
+
+
+def test_heightfield_small_textures_off(ctx):
+    sc = scenes.scene_heightfield_1280x720(n=97)
+    sc = dataclasses.replace(sc, width=643, height=357)  # width not a multiple of 4
+    compare(ctx, sc, flags=sc.flags & ~gr.SHOW_TEXTURES)
+
+
+def test_heightfield_no_cull_no_clip(ctx):
+    sc = scenes.scene_heightfield_1280x720(n=129)
+    compare(ctx, sc, flags=sc.flags & ~(gr.BACKFACE_CULLING | gr.FRUSTUM_CLIPPING))
+
+
+def test_icospheres_vertex_colours(ctx):
+    sc = scenes.scene_icospheres_1920x1080(count=12, levels=(2, 3))
+    sc = dataclasses.replace(sc, width=960, height=540)
+    compare(ctx, sc)
+
+
+def test_camera_inside_sphere_near_plane(ctx):
+    m = scenes.icosphere(3)
+    sc = scenes.SceneData("inside", 320, 240, [scenes.ObjectData(m, scale=(2.0, 2.0, 2.0))],
+                          scenes.CameraData((0.1, 0.2, 0.3), (0.3, -0.2, -1.0), (0.0, 1.0, 0.0)), [],
+                          gr.FLAGS_DEFAULT & ~gr.BACKFACE_CULLING)
+    compare(ctx, sc)
+
+
+def test_non_pow2_and_solid_textures(ctx):
+    m = scenes.heightfield(65, extent=1.5, seed=3)
+    tex_img = scenes.random_texture(12, 10, seed=5, scale=3.0)  # not a power of two: % path
+    solid = scenes.TextureData.solid((10, 200, 30, 255))
+    m.tex = (np.arange(m.nf) % 3 - 1).astype(np.int32)  # -1 nil, 0 image, 1 solid
+    cam = scenes.CameraData((0.0, 0.6, 1.8), (0.0, -0.5, -1.0), (0.0, 1.0, 0.0))
+    sc = scenes.SceneData("textures", 400, 300, [scenes.ObjectData(m)], cam, [tex_img, solid],
+                          gr.FLAGS_DEFAULT | gr.FLAT_SHADING)
+    compare(ctx, sc)
+
+
+def test_multi_object_depth_ties(ctx):
+    # the same mesh drawn twice at the same place: every pixel is a depth tie and
+    # the later object must win (rasterizer.go:156 uses >=)
+    m = scenes.icosphere(2)
+    m2 = dataclasses.replace(m, vcolor=np.full((m.nv, 3), 0.25, np.float32))
+    objs = [scenes.ObjectData(m), scenes.ObjectData(m2)]
+    sc = scenes.SceneData("ties", 256, 256, objs, scenes.CameraData((0, 0, 3.0), (0, 0, -1.0), (0, 1, 0)), [],
+                          gr.FLAGS_DEFAULT)
+    rgba, z, _ = compare(ctx, sc)
+    covered = z > -1
+    assert (rgba[covered][:, 3] == 255).all()
+
+
+def test_empty_and_offscreen(ctx):
+    m = scenes.icosphere(1)
+    sc = scenes.SceneData("behind", 128, 96, [scenes.ObjectData(m, translation=(0.0, 0.0, 10.0))],
+                          scenes.CameraData((0, 0, 0), (0, 0, -1.0), (0, 1, 0)), [], gr.FLAGS_DEFAULT)
+    rgba, z, tpf = compare(ctx, sc)
+    assert tpf == 0 and (z == -1).all()
+    sc0 = dataclasses.replace(sc, objects=[])
+    compare(ctx, sc0)
+
+
+def test_renderer_api_matches_low_level(ctx):
+    sc = scenes.scene_uvsphere_640x360()
+    up = gr.UploadedScene(ctx, sc)
+    rgba, z, tpf = up.render()
+    r = gr.Renderer(ctx, sc.width, sc.height)
+    r.set_fov(up.fov)
+    assert r.BackfaceCulling and r.Lighting and not r.FlatShading
+    r.draw([gr.Object(up.mesh_handles[0])], gr.Camera(*[getattr(sc.camera, k) for k in ("position", "direction", "up")]))
+    assert r.TPF == tpf
+    assert np.array_equal(r.pixels(), rgba)
+    assert np.array_equal(r.zbuffer().view(np.uint32), z.view(np.uint32))
+    r.close()
