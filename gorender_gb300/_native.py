@@ -33,7 +33,7 @@ EXPORTS = [
     "gr_renderer_set_fov", "gr_renderer_set_light", "gr_renderer_draw", "gr_renderer_read",
     "gr_renderer_tpf", "gr_context_event_record", "gr_context_event_elapsed", "gr_context_flush_l2",
     "gr_context_last_launches", "gr_context_last_transfer_bytes", "gr_draw_profiled", "gr_host_alloc",
-    "gr_host_free",
+    "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning",
 ]
 
 
@@ -115,6 +115,8 @@ def lib() -> C.CDLL:
             "gr_draw_profiled": [vp, C.POINTER(DrawItem), i32, C.POINTER(FrameParams), vp, vp, fp],
             "gr_host_alloc": [C.c_int64, C.POINTER(vp)],
             "gr_host_free": [vp],
+            "gr_context_set_tuning": [vp, i32, i32],
+            "gr_context_get_tuning": [vp, C.POINTER(i32), C.POINTER(i32)],
         }
         for name, args in sig.items():
             f = getattr(L, name)

@@ -89,6 +89,10 @@ struct gr_context {
   uint32_t tiles_cap = 0;
   uint32_t* big = nullptr;
   uint32_t big_cap = 0;
+  unsigned long long* gkey = nullptr;  // merged keys of tiles split over several CTAs
+  uint32_t* tile_done = nullptr;
+  uint32_t gkey_tiles = 0;
+  uint32_t slice_entries = kDefaultSliceEntries;
   DevWork* work = nullptr;
   DevResult* d_result = nullptr;
   DevResult* h_result = nullptr;  // pinned
@@ -104,6 +108,7 @@ struct gr_context {
   int32_t pending = GR_OK;
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes of the last draw
   uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0;
+  int tile_shift = kDefaultTileShift;  // raster tile size (autotuned per workload)
 };
 
 struct gr_renderer {
@@ -208,6 +213,14 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
     c->tiles_cap = 0; c->bin_cap = 0;
     if ((st = dev_alloc(&c->bins, (size_t)nt * nc)) || (st = dev_alloc(&c->bin_count, nt))) return st;
     CK(cudaMemsetAsync(c->bin_count, 0, sizeof(uint32_t) * nt, c->stream));
+    if (nt > c->gkey_tiles) {
+      dev_free(c->gkey); dev_free(c->tile_done);
+      c->gkey_tiles = 0;
+      if ((st = dev_alloc(&c->gkey, (size_t)nt * 1024)) || (st = dev_alloc(&c->tile_done, nt))) return st;
+      CK(cudaMemsetAsync(c->gkey, 0, sizeof(unsigned long long) * nt * 1024, c->stream));
+      CK(cudaMemsetAsync(c->tile_done, 0, sizeof(uint32_t) * nt, c->stream));
+      c->gkey_tiles = nt;
+    }
     c->tiles_cap = nt;
     c->bin_cap = nc;
   }
@@ -298,8 +311,9 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
     blocks += (mr.nf + kProjectThreads - 1) / kProjectThreads;
   }
   if (faces >= (1ull << 28)) return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces in one frame");
-  const int tiles_x = (p->width + kTileSize - 1) / kTileSize;
-  const int tiles_y = (p->height + kTileSize - 1) / kTileSize;
+  const int ts = 1 << c->tile_shift;
+  const int tiles_x = (p->width + ts - 1) / ts;
+  const int tiles_y = (p->height + ts - 1) / ts;
   if ((st = ensure_frame_buffers(c, faces, (uint32_t)(tiles_x * tiles_y)))) return st;
   if (live) CK(cudaMemcpyAsync(c->d_items, c->h_items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
   c->h2d_bytes = (int64_t)sizeof(DevItem) * live;
@@ -312,6 +326,7 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   a.flags = p->flags;
   a.tiles_x = tiles_x;
   a.tiles_y = tiles_y;
+  a.tile_shift = c->tile_shift;
   a.num_items = live;
   a.total_blocks = blocks;
   a.bin_cap = c->bin_cap;
@@ -331,6 +346,9 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   a.bins = c->bins;
   a.bin_count = c->bin_count;
   a.big = c->big;
+  a.gkey = c->gkey;
+  a.tile_done = c->tile_done;
+  a.slice_entries = c->slice_entries;
   a.work = c->work;
   a.result = c->d_result;
   out.faces = faces;
@@ -450,6 +468,7 @@ int32_t gr_context_destroy(gr_context* c) {
   if (c->h_items) cudaFreeHost(c->h_items);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->big);
+  dev_free(c->gkey); dev_free(c->tile_done);
   dev_free(c->work); dev_free(c->d_result);
   if (c->h_result) cudaFreeHost(c->h_result);
   dev_free(c->fb_rgba); dev_free(c->fb_z);
@@ -804,6 +823,33 @@ int32_t gr_context_flush_l2(gr_context* c, int64_t bytes) {
     c->flush_bytes = (size_t)bytes;
   }
   CK(cudaMemsetAsync(c->flush_buf, c->last_launches & 0xFF, (size_t)bytes, c->stream));
+  return GR_OK;
+}
+
+int32_t gr_context_set_tuning(gr_context* c, int32_t tile_size, int32_t bin_capacity) {
+  if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  if (tile_size != 0 && tile_size != 16 && tile_size != 32)
+    return fail(GR_ERR_INVALID_ARGUMENT, "tile size must be 16 or 32 (0 keeps it)");
+  if (bin_capacity < 0) return fail(GR_ERR_INVALID_ARGUMENT, "negative bin capacity");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  if (tile_size) c->tile_shift = tile_size == 16 ? 4 : 5;
+  if (bin_capacity) {
+    // takes effect at the next draw; the buffers are re-sized to exactly this
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->bins);
+    dev_free(c->bin_count);
+    c->tiles_cap = 0;
+    c->bin_cap = 0;
+    c->want_bin_cap = (uint32_t)bin_capacity;
+  }
+  return GR_OK;
+}
+
+int32_t gr_context_get_tuning(gr_context* c, int32_t* tile_size, int32_t* bin_capacity) {
+  if (!c || !tile_size || !bin_capacity) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *tile_size = 1 << c->tile_shift;
+  *bin_capacity = (int32_t)c->bin_cap;
   return GR_OK;
 }
 

@@ -7,15 +7,15 @@
 
 namespace gr {
 
-constexpr int kTileShift = 5;                 // 32 x 32 pixel raster tiles
-constexpr int kTileSize = 1 << kTileShift;
+constexpr int kDefaultTileShift = 5;          // 32 x 32 pixel raster tiles (16 x 16: shift 4)
 constexpr int kMaxDim = 16384;                // narrow edge-function bound
 constexpr int kNarrowLimit = 16384;           // |screen coordinate| < 2^14 => int32 edge math
 constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes fans into <= 7
 constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
 constexpr int kProjectThreads = 256;
-constexpr int kRasterThreads = 256;
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
+constexpr int kRasterMaxSlices = 8;           // CTAs that may share one tile's bin
+constexpr int kDefaultSliceEntries = 128;     // bin entries per slice before a tile is split
 
 // Texture table entry (texture.go:19-26).
 struct DevTex {
@@ -100,6 +100,7 @@ struct FrameArgs {
   int W, H;
   uint32_t flags;
   int tiles_x, tiles_y;
+  int tile_shift;                   // raster tile = (1 << tile_shift)^2 pixels (4 or 5)
   int num_items;
   int total_blocks;
   uint32_t bin_cap;
@@ -120,6 +121,9 @@ struct FrameArgs {
   uint32_t* bins;                   // tiles x bin_cap record indices
   uint32_t* bin_count;              // per tile
   uint32_t* big;                    // multi-tile record queue
+  unsigned long long* gkey;         // tiles x 1024 merged visibility keys of split tiles (zero when idle)
+  uint32_t* tile_done;              // per tile: slices finished (zero when idle)
+  uint32_t slice_entries;           // bin entries per slice
   DevWork* work;
   DevResult* result;
   uint32_t* out_rgba;               // H x W RGBA8

@@ -343,10 +343,13 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   const bool valid = f < it.nf;
   const unsigned lane = lane_id();
 
-  PV poly[9];
-  PV tmp[9];
+  // mode 0: nothing to draw; 1: the face itself (registers only);
+  // 2: a clipped polygon (local memory, rare)
+  int mode = 0;
   int pcount = 0;
   int tex = -1;
+  PV p0, p1, p2;
+  PV poly[9];
   if (valid) {
     const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
     V4 v0 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i0));
@@ -362,7 +365,22 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
       float d = fa(fa(fm(nx, fs(0.0f, v0.x)), fm(ny, fs(0.0f, v0.y))), fm(nz, fs(0.0f, v0.z)));
       draw = d > 0.0f;
     }
-    if (draw) {
+    // Frustum clipping (renderer.go:349-359).  At the first plane, in clipping
+    // order, where not all three vertices are inside: all outside means the
+    // polygon reaching that plane is still the face itself (every earlier pass
+    // only rotated it), so ClipTriangle returns no triangle; a mix needs the
+    // general clipper.  With no such plane the six passes rotate the face back
+    // to itself and it passes through unchanged.
+    int clip = 0;  // 0 pass through, 1 rejected, 2 general
+    if (draw && (fl & 0x01u) && vis != 2) {
+      for (int i = 0; i < 6; ++i) {
+        const int m = (int)plane_inside(i, v0) + (int)plane_inside(i, v1) + (int)plane_inside(i, v2);
+        if (m == 3) continue;
+        clip = (m == 0) ? 1 : 2;
+        break;
+      }
+    }
+    if (draw && clip != 1) {
       float in0, in1, in2;
       if (fl & 0x08u) {  // Lighting (renderer.go:326-346)
         if (it.nn != 0 && !(fl & 0x10u)) {
@@ -386,57 +404,65 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
       } else {
         in0 = in1 = in2 = 0.5f;
       }
-      poly[0].p = v0; poly[1].p = v1; poly[2].p = v2;
-      poly[0].in = in0; poly[1].in = in1; poly[2].in = in2;
+      p0.p = v0; p1.p = v1; p2.p = v2;
+      p0.in = in0; p1.in = in1; p2.in = in2;
       if (it.uv) {
-        const float* uv = it.uv + 6 * (size_t)f;
-        poly[0].u = __ldg(uv); poly[0].v = __ldg(uv + 1);
-        poly[1].u = __ldg(uv + 2); poly[1].v = __ldg(uv + 3);
-        poly[2].u = __ldg(uv + 4); poly[2].v = __ldg(uv + 5);
+        const float2* uv = reinterpret_cast<const float2*>(it.uv + 6 * (size_t)f);
+        const float2 t0 = __ldg(uv), t1 = __ldg(uv + 1), t2 = __ldg(uv + 2);
+        p0.u = t0.x; p0.v = t0.y; p1.u = t1.x; p1.v = t1.y; p2.u = t2.x; p2.v = t2.y;
       } else {
-        poly[0].u = poly[0].v = poly[1].u = poly[1].v = poly[2].u = poly[2].v = 0.0f;
+        p0.u = p0.v = p1.u = p1.v = p2.u = p2.v = 0.0f;
       }
       if (it.vcol) {
         const float* c0 = it.vcol + 3 * (size_t)i0;
         const float* c1 = it.vcol + 3 * (size_t)i1;
         const float* c2 = it.vcol + 3 * (size_t)i2;
-        poly[0].r = __ldg(c0); poly[0].g = __ldg(c0 + 1); poly[0].b = __ldg(c0 + 2);
-        poly[1].r = __ldg(c1); poly[1].g = __ldg(c1 + 1); poly[1].b = __ldg(c1 + 2);
-        poly[2].r = __ldg(c2); poly[2].g = __ldg(c2 + 1); poly[2].b = __ldg(c2 + 2);
+        p0.r = __ldg(c0); p0.g = __ldg(c0 + 1); p0.b = __ldg(c0 + 2);
+        p1.r = __ldg(c1); p1.g = __ldg(c1 + 1); p1.b = __ldg(c1 + 2);
+        p2.r = __ldg(c2); p2.g = __ldg(c2 + 1); p2.b = __ldg(c2 + 2);
       } else {
-        poly[0].r = poly[0].g = poly[0].b = poly[1].r = poly[1].g = poly[1].b = 0.0f;
-        poly[2].r = poly[2].g = poly[2].b = 0.0f;
+        p0.r = p0.g = p0.b = p1.r = p1.g = p1.b = p2.r = p2.g = p2.b = 0.0f;
       }
       int t = it.tex ? __ldg(it.tex + f) : -1;
       tex = ((fl & 0x20u) && t >= 0) ? t : (it.vcol ? -2 : -1);  // renderer.go:176-178
-      pcount = 3;
-      if ((fl & 0x01u) && vis != 2) {  // FrustumClipping (renderer.go:349-359)
-        bool all_in = true;
-        for (int i = 0; i < 6 && all_in; ++i)
-          all_in = plane_inside(i, v0) && plane_inside(i, v1) && plane_inside(i, v2);
-        if (!all_in) {  // six all-inside passes rotate the triangle back to itself
-          pcount = clip_polygon(poly, tmp);
-          if (pcount < 0) {
-            atomicOr(&a.work->error, 1u);
-            pcount = 0;
-          }
+      mode = 1;
+      if (clip == 2) {
+        PV tmp[9];
+        poly[0] = p0; poly[1] = p1; poly[2] = p2;
+        pcount = clip_polygon(poly, tmp);
+        if (pcount < 0) {
+          atomicOr(&a.work->error, 1u);
+          pcount = 0;
         }
+        mode = pcount >= 3 ? 2 : 0;
       }
     }
   }
 
   // Divide + screen map per polygon vertex, bin test and setup per fan triangle.
+  SV s0, s1, s2;
   SV sv[9];
   unsigned fanmask = 0;
   int ntpf = 0;
   const float Wf = (float)a.W, Hf = (float)a.H;
-  for (int k = 0; k < pcount; ++k) sv[k] = to_screen(poly[k], a.S);
-  for (int t = 0; t + 2 < pcount; ++t) {
-    if (!bin_test(sv[0], sv[t + 1], sv[t + 2], Wf, Hf)) continue;
-    ++ntpf;
-    Setup s;
-    // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
-    if ((fl & 0x02u) && setup_tri(sv[0], sv[t + 1], sv[t + 2], a.W, a.H, s)) fanmask |= 1u << t;
+  if (mode == 1) {
+    s0 = to_screen(p0, a.S);
+    s1 = to_screen(p1, a.S);
+    s2 = to_screen(p2, a.S);
+    if (bin_test(s0, s1, s2, Wf, Hf)) {
+      ntpf = 1;
+      Setup s;
+      // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
+      if ((fl & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s)) fanmask = 1u;
+    }
+  } else if (mode == 2) {
+    for (int k = 0; k < pcount; ++k) sv[k] = to_screen(poly[k], a.S);
+    for (int t = 0; t + 2 < pcount; ++t) {
+      if (!bin_test(sv[0], sv[t + 1], sv[t + 2], Wf, Hf)) continue;
+      ++ntpf;
+      Setup s;
+      if ((fl & 0x02u) && setup_tri(sv[0], sv[t + 1], sv[t + 2], a.W, a.H, s)) fanmask |= 1u << t;
+    }
   }
 
   // TPF: one atomic per warp.
@@ -471,8 +497,14 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
     if (has) ++my;
     uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
     if (ok) {
+      SV q0 = s0, q1 = s1, q2 = s2;
+      if (mode == 2) {
+        q0 = sv[0];
+        q1 = sv[t + 1];
+        q2 = sv[t + 2];
+      }
       Setup s;
-      setup_tri(sv[0], sv[t + 1], sv[t + 2], a.W, a.H, s);
+      setup_tri(q0, q1, q2, a.W, a.H, s);
       uint32_t okey = face_key + (uint32_t)t + 1u;
       s.r.key = okey | (s.wide ? 0x80000000u : 0u);
       const int4* src = reinterpret_cast<const int4*>(&s.r);
@@ -484,14 +516,11 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
 #pragma unroll
         for (int q = 0; q < 5; ++q) wd[q] = ws[q];
       }
-      const SV& p0 = sv[0];
-      const SV& p1 = sv[t + 1];
-      const SV& p2 = sv[t + 2];
       TriShade sh;
-      sh.u0w = fd(p0.u, p0.W); sh.v0w = fd(p0.v, p0.W);
-      sh.u1w = fd(p1.u, p1.W); sh.v1w = fd(p1.v, p1.W);
-      sh.u2w = fd(p2.u, p2.W); sh.v2w = fd(p2.v, p2.W);
-      sh.i0 = p0.in; sh.i1 = p1.in; sh.i2 = p2.in;
+      sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);
+      sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
+      sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
+      sh.i0 = q0.in; sh.i1 = q1.in; sh.i2 = q2.in;
       sh.tex = tex;
       sh.pad[0] = sh.pad[1] = 0.0f;
       const float4* ss = reinterpret_cast<const float4*>(&sh);
@@ -499,15 +528,15 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
       sd[0] = ss[0]; sd[1] = ss[1]; sd[2] = ss[2];
       if (tex == -2) {
         TriColor* c = a.tcol + r;
-        c->c[0] = p0.r; c->c[1] = p0.g; c->c[2] = p0.b;
-        c->c[3] = p1.r; c->c[4] = p1.g; c->c[5] = p1.b;
-        c->c[6] = p2.r; c->c[7] = p2.g; c->c[8] = p2.b;
+        c->c[0] = q0.r; c->c[1] = q0.g; c->c[2] = q0.b;
+        c->c[3] = q1.r; c->c[4] = q1.g; c->c[5] = q1.b;
+        c->c[6] = q2.r; c->c[7] = q2.g; c->c[8] = q2.b;
       }
       if (okey < a.key_cap) a.rec_of_key[okey] = r;
-      tx0 = (uint32_t)s.r.bx0 >> kTileShift;
-      tx1 = (uint32_t)s.r.bx1 >> kTileShift;
-      ty0 = (uint32_t)s.r.by0 >> kTileShift;
-      ty1 = (uint32_t)s.r.by1 >> kTileShift;
+      tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
+      tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
+      ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
+      ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
     }
     const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
     // single-tile triangles: warp-aggregated append per distinct tile
@@ -552,12 +581,14 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
 // k_bin_big: one CTA per multi-tile triangle
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
+  const int sh = a.tile_shift;
+  const int ts = 1 << sh;
   const uint32_t nbig = min(*(volatile uint32_t*)&a.work->nbig, a.big_cap);
   for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
     const uint32_t r = a.big[q];
     const TriRaster t = a.rast[r];
-    const uint32_t tx0 = (uint32_t)t.bx0 >> kTileShift, tx1 = (uint32_t)t.bx1 >> kTileShift;
-    const uint32_t ty0 = (uint32_t)t.by0 >> kTileShift, ty1 = (uint32_t)t.by1 >> kTileShift;
+    const uint32_t tx0 = (uint32_t)t.bx0 >> sh, tx1 = (uint32_t)t.bx1 >> sh;
+    const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
     const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
     const bool wide = (t.key & 0x80000000u) != 0;
     for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
@@ -565,13 +596,13 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
       if (!wide) {
         // conservative reject: an edge that is >= 0 over the whole
         // tile-clipped box excludes every pixel of it
-        const long long X0 = max((int)(tx << kTileShift), (int)t.bx0);
-        const long long X1 = min((int)((tx << kTileShift) + kTileSize - 1), (int)t.bx1);
-        const long long Y0 = max((int)(ty << kTileShift), (int)t.by0);
-        const long long Y1 = min((int)((ty << kTileShift) + kTileSize - 1), (int)t.by1);
-        const long long e01 = t.c01 + min(t.a01 * X0, t.a01 * X1) + min(t.b01 * Y0, t.b01 * Y1);
-        const long long e12 = t.c12 + min(t.a12 * X0, t.a12 * X1) + min(t.b12 * Y0, t.b12 * Y1);
-        const long long e20 = t.c20 + min(t.a20 * X0, t.a20 * X1) + min(t.b20 * Y0, t.b20 * Y1);
+        const int X0 = max((int)(tx << sh), (int)t.bx0);
+        const int X1 = min((int)(tx << sh) + ts - 1, (int)t.bx1);
+        const int Y0 = max((int)(ty << sh), (int)t.by0);
+        const int Y1 = min((int)(ty << sh) + ts - 1, (int)t.by1);
+        const int e01 = t.c01 + min(t.a01 * X0, t.a01 * X1) + min(t.b01 * Y0, t.b01 * Y1);
+        const int e12 = t.c12 + min(t.a12 * X0, t.a12 * X1) + min(t.b12 * Y0, t.b12 * Y1);
+        const int e20 = t.c20 + min(t.a20 * X0, t.a20 * X1) + min(t.b20 * Y0, t.b20 * Y1);
         if (e01 >= 0 || e12 >= 0 || e20 >= 0) continue;
       }
       const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
@@ -581,7 +612,7 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_raster: one CTA per 32x32 tile
+// k_raster: one CTA per TS x TS tile
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t tex_sample(const DevTex& t, float u, float v) {
   // Texture.Sample (texture.go:69-89)
@@ -632,32 +663,158 @@ __device__ __forceinline__ void edges_at(const TriRaster& t, const TriWide* wide
   }
 }
 
-__device__ __forceinline__ void raster_pixel(unsigned long long* skey, const TriRaster& t, const TriWide* wide,
-                                             uint32_t r, int x, int y, int tx0, int ty0) {
+template <int TS>
+struct RasterShape {
+  static constexpr int kThreads = TS * TS / 4;  // 4 pixels per thread in the resolve
+  static constexpr int kStride = TS + 8;        // padded key row: 8x4 warp blocks hit disjoint banks
+  static constexpr int kWarps = kThreads / 32;
+};
+
+// Exact depth test of one covered pixel: zRec in the reference's order,
+// then a 64-bit max of (ordered zRec, draw-order key) into the tile's keys.
+template <int TS>
+__device__ __forceinline__ void depth_candidate(unsigned long long* skey, const TriRaster& t, const TriWide* wide,
+                                                uint32_t r, int x, int y, int tx0, int ty0) {
   bool inside;
   float e12f, e20f;
   edges_at(t, wide, r, x, y, inside, e12f, e20f);
-  if (!inside) return;
   float al, be, ga;
   float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
   if (!(z >= -1.0f)) return;  // rasterizer.go:156 against the cleared Z of -1
   unsigned long long k = depth_key(z, t.key);
-  unsigned long long* p = skey + (y - ty0) * kTileSize + (x - tx0);
+  unsigned long long* p = skey + (y - ty0) * RasterShape<TS>::kStride + (x - tx0);
   if (k > *(volatile unsigned long long*)p) atomicMax(p, k);
 }
 
-__global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameArgs a) {
-  __shared__ unsigned long long skey[kTileSize * kTileSize];
-  const int tid = threadIdx.x;
-  const uint32_t tile = blockIdx.x;
-  const int tx0 = (int)(tile % (uint32_t)a.tiles_x) << kTileShift;
-  const int ty0 = (int)(tile / (uint32_t)a.tiles_x) << kTileShift;
-  const int tx1 = min(tx0 + kTileSize - 1, a.W - 1);
-  const int ty1 = min(ty0 + kTileSize - 1, a.H - 1);
+// Coverage test of one pixel (rasterizer.go:147).
+__device__ __forceinline__ bool covers(const TriRaster& t, const TriWide* wide, uint32_t r, int x, int y) {
+  if (!(t.key & 0x80000000u)) {
+    return t.a01 * x + t.b01 * y + t.c01 < 0 && t.a12 * x + t.b12 * y + t.c12 < 0 &&
+           t.a20 * x + t.b20 * y + t.c20 < 0;
+  }
+  bool inside;
+  float e12f, e20f;
+  edges_at(t, wide, r, x, y, inside, e12f, e20f);
+  return inside;
+}
 
-  for (int i = tid; i < kTileSize * kTileSize; i += kRasterThreads) skey[i] = BG_KEY;
+// Minimum of a narrow edge function over the pixel box [X0,X1] x [Y0,Y1].
+__device__ __forceinline__ int edge_min(int a, int b, int c, int X0, int X1, int Y0, int Y1) {
+  return c + min(a * X0, a * X1) + min(b * Y0, b * Y1);
+}
+
+// Per-warp queue of covered pixels awaiting the exact depth test, so that the
+// division-heavy part runs with every lane busy.  Each entry names a slot of
+// the warp's triangle table (records staged in shared memory, so a drain
+// reads no global memory) and a pixel.  qn is warp-uniform; capacity 64: the
+// warp drains 32 whenever qn >= 32.
+template <int TS>
+struct CandQueue {
+  uint32_t* ent;        // slot | x << 8 | y << 20
+  const TriRaster* tri; // the warp's triangle table (kSlots entries)
+  const uint32_t* rec;  // record index per slot (for int64 edge coefficients)
+  int qn;
+
+  __device__ __forceinline__ void run(uint32_t e, unsigned long long* skey, const FrameArgs& a, int tx0, int ty0) {
+    const uint32_t slot = e & 0xFFu;
+    const TriRaster t = tri[slot];
+    depth_candidate<TS>(skey, t, a.wide, rec[slot], tx0 + (int)((e >> 8) & 0xFFFu), ty0 + (int)(e >> 20), tx0,
+                        ty0);
+  }
+
+  __device__ __forceinline__ void push(bool covered, uint32_t slot, int x, int y, unsigned long long* skey,
+                                       const FrameArgs& a, int tx0, int ty0) {
+    const unsigned lane = lane_id();
+    const unsigned m = __ballot_sync(FULL_MASK, covered);
+    if (covered) ent[qn + __popc(m & ((1u << lane) - 1u))] = slot | ((uint32_t)x << 8) | ((uint32_t)y << 20);
+    qn += __popc(m);
+    if (qn >= 32) {
+      __syncwarp();
+      run(ent[lane], skey, a, tx0, ty0);
+      const int rest = qn - 32;
+      uint32_t e = 0;
+      if ((int)lane < rest) e = ent[32 + lane];
+      __syncwarp();
+      if ((int)lane < rest) ent[lane] = e;
+      __syncwarp();
+      qn = rest;
+    }
+  }
+
+  __device__ __forceinline__ void flush(unsigned long long* skey, const FrameArgs& a, int tx0, int ty0) {
+    const unsigned lane = lane_id();
+    __syncwarp();
+    if ((int)lane < qn) run(ent[lane], skey, a, tx0, ty0);
+    __syncwarp();
+    qn = 0;
+  }
+};
+
+
+// Walks the 8x4 blocks j = j0, j0 + step, ... of the footprint [bx0,bx1] x
+// [by0,by1] of the triangle in table slot `slot`, one pixel per lane.  Blocks
+// that one edge excludes entirely are skipped before any per-pixel work;
+// covered pixels go to the warp's queue.
+template <int TS>
+__device__ __forceinline__ void walk_blocks(CandQueue<TS>& q, unsigned long long* skey, const FrameArgs& a,
+                                            const TriRaster& tt, uint32_t rr, uint32_t slot, int bx0, int bx1,
+                                            int by0, int by1, int j0, int step, int tx0, int ty0) {
+  const unsigned lane = lane_id();
+  const bool narrow = !(tt.key & 0x80000000u);
+  const int px = (int)(lane & 7u), py = (int)(lane >> 3);
+  const int nbx = (bx1 - bx0 + 8) >> 3;
+  const int nblk = nbx * ((by1 - by0 + 4) >> 2);
+  for (int j = j0; j < nblk; j += step) {
+    const int bj = j / nbx;
+    const int x8 = bx0 + ((j - bj * nbx) << 3), y4 = by0 + (bj << 2);
+    const int X1 = min(x8 + 7, bx1), Y1 = min(y4 + 3, by1);
+    if (narrow && (edge_min(tt.a01, tt.b01, tt.c01, x8, X1, y4, Y1) >= 0 ||
+                   edge_min(tt.a12, tt.b12, tt.c12, x8, X1, y4, Y1) >= 0 ||
+                   edge_min(tt.a20, tt.b20, tt.c20, x8, X1, y4, Y1) >= 0))
+      continue;
+    const int x = x8 + px, y = y4 + py;
+    const bool c = x <= X1 && y <= Y1 && covers(tt, a.wide, rr, x, y);
+    q.push(c, slot, x - tx0, y - ty0, skey, a, tx0, ty0);
+  }
+}
+
+template <int TS>
+__global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const FrameArgs a) {
+  constexpr int kThreads = RasterShape<TS>::kThreads;
+  constexpr int kStride = RasterShape<TS>::kStride;
+  constexpr int kWarps = RasterShape<TS>::kWarps;
+  constexpr uint32_t kLargeCap = 128;     // queued large triangles per round
+  constexpr int kLaneArea = 256;          // footprints up to 256 pixels: one lane each
+  constexpr int kSlots = 64;              // triangle table: 32 lane slots + 32 for large ones
+  constexpr uint32_t kMaxSlices = kRasterMaxSlices;
+  __shared__ __align__(16) unsigned long long skey[TS * kStride];
+  __shared__ __align__(16) TriRaster s_tri[kWarps][kSlots];
+  __shared__ uint32_t s_trec[kWarps][kSlots];
+  __shared__ uint32_t s_ent[kWarps][64];
+  __shared__ uint32_t s_large[kLargeCap + kThreads];
+  __shared__ uint32_t s_next, s_nlarge, s_last;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  // A tile's bin is split into up to kMaxSlices slices, one CTA each; CTAs of
+  // one tile are adjacent in launch order.
+  const uint32_t tile = blockIdx.x / kMaxSlices;
+  const uint32_t slice = blockIdx.x % kMaxSlices;
   const uint32_t count = a.bin_count[tile];
   const uint32_t n = min(count, a.bin_cap);
+  const uint32_t nslices = min((uint32_t)kMaxSlices, max(1u, (n + a.slice_entries - 1) / a.slice_entries));
+  if (slice >= nslices) return;  // whole CTA: this tile needs fewer slices
+  const uint32_t per = (((n + nslices - 1) / nslices) + 31u) & ~31u;
+  const uint32_t lo = min(n, slice * per), hi = min(n, lo + per);
+  const int tx0 = (int)(tile % (uint32_t)a.tiles_x) * TS;
+  const int ty0 = (int)(tile / (uint32_t)a.tiles_x) * TS;
+  const int tx1 = min(tx0 + TS - 1, a.W - 1);
+  const int ty1 = min(ty0 + TS - 1, a.H - 1);
+
+  for (int i = tid; i < TS * kStride; i += kThreads) skey[i] = BG_KEY;
+  if (tid == 0) {
+    s_next = lo;
+    s_nlarge = 0;
+  }
   if (tid == 0 && blockIdx.x == 0) {
     // publish and reset the frame counters (all appends are complete)
     DevWork* w = a.work;
@@ -673,59 +830,131 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameArgs a) {
   __syncthreads();
 
   const unsigned lane = lane_id();
-  const int warp = tid >> 5;
   const uint32_t* bin = a.bins + (size_t)tile * a.bin_cap;
-  for (uint32_t b = (uint32_t)warp * 32u; b < n; b += kRasterThreads) {
-    const uint32_t i = b + lane;
-    const bool valid = i < n;
-    uint32_t r = 0;
-    int lx0 = 0, lx1 = -1, ly0 = 0, ly1 = -1;
-    TriRaster t;
-    if (valid) {
-      r = bin[i];
-      t = a.rast[r];
-      lx0 = max((int)t.bx0, tx0); lx1 = min((int)t.bx1, tx1);
-      ly0 = max((int)t.by0, ty0); ly1 = min((int)t.by1, ty1);
-    }
-    const int area = (lx1 >= lx0 && ly1 >= ly0) ? (lx1 - lx0 + 1) * (ly1 - ly0 + 1) : 0;
-    const bool small = valid && area > 0 && area <= 16;
-    if (small) {
-      for (int y = ly0; y <= ly1; ++y)
-        for (int x = lx0; x <= lx1; ++x) raster_pixel(skey, t, a.wide, r, x, y, tx0, ty0);
-    }
-    // larger footprints: the whole warp walks 8x8 blocks, 2 pixels per lane
-    unsigned bigm = __ballot_sync(FULL_MASK, valid && area > 16);
-    while (bigm) {
-      const int src = __ffs(bigm) - 1;
-      bigm &= bigm - 1;
-      const uint32_t rr = __shfl_sync(FULL_MASK, r, src);
-      const int bx0 = __shfl_sync(FULL_MASK, lx0, src), bx1 = __shfl_sync(FULL_MASK, lx1, src);
-      const int by0 = __shfl_sync(FULL_MASK, ly0, src), by1 = __shfl_sync(FULL_MASK, ly1, src);
-      const TriRaster tt = a.rast[rr];
-      const int px = (int)(lane & 7u), py = (int)(lane >> 3);
-      for (int y8 = by0; y8 <= by1; y8 += 8)
-        for (int x8 = bx0; x8 <= bx1; x8 += 8) {
-          const int x = x8 + px;
-          if (x > bx1) continue;
-          const int y = y8 + py;
-          if (y <= by1) raster_pixel(skey, tt, a.wide, rr, x, y, tx0, ty0);
-          if (y + 4 <= by1) raster_pixel(skey, tt, a.wide, rr, x, y + 4, tx0, ty0);
+  TriRaster* tri = s_tri[warp];
+  uint32_t* trec = s_trec[warp];
+  CandQueue<TS> q{s_ent[warp], tri, trec, 0};
+  for (;;) {
+    // Phase 1: warps take 32 bin entries at a time from a shared cursor.
+    // Footprints up to kLaneArea pixels run one lane per triangle in a
+    // converged loop (so covered pixels can be queued warp-synchronously);
+    // larger or int64 triangles are queued for the whole CTA.
+    for (;;) {
+      if (*(volatile uint32_t*)&s_nlarge >= kLargeCap) break;
+      uint32_t b = 0;
+      if (lane == 0) b = atomicAdd(&s_next, 32u);
+      b = __shfl_sync(FULL_MASK, b, 0);
+      if (b >= hi) break;
+      const uint32_t i = b + lane;
+      const bool valid = i < hi;
+      uint32_t r = 0;
+      int lx0 = 0, lx1 = -1, ly0 = 0, ly1 = -1;
+      TriRaster t;
+      if (valid) {
+        r = bin[i];
+        t = a.rast[r];
+        lx0 = max((int)t.bx0, tx0); lx1 = min((int)t.bx1, tx1);
+        ly0 = max((int)t.by0, ty0); ly1 = min((int)t.by1, ty1);
+      }
+      const bool live = valid && lx1 >= lx0 && ly1 >= ly0;
+      const int area = live ? (lx1 - lx0 + 1) * (ly1 - ly0 + 1) : 0;
+      const bool by_lane = live && area <= kLaneArea && !(t.key & 0x80000000u);
+      const bool large = live && !by_lane;
+      const unsigned lm = __ballot_sync(FULL_MASK, large);
+      if (lm) {
+        uint32_t qb = 0;
+        const int ldr = __ffs(lm) - 1;
+        if ((int)lane == ldr) qb = atomicAdd(&s_nlarge, (uint32_t)__popc(lm));
+        qb = __shfl_sync(FULL_MASK, qb, ldr);
+        if (large) s_large[qb + __popc(lm & ((1u << lane) - 1u))] = r;
+      }
+      if (by_lane) {
+        tri[lane] = t;
+        trec[lane] = r;
+      }
+      const int my = by_lane ? area : 0;
+      const int iters = __reduce_max_sync(FULL_MASK, my);
+      int x = lx0, y = ly0;
+      for (int it = 0; it < iters; ++it) {
+        const bool c = it < my && t.a01 * x + t.b01 * y + t.c01 < 0 && t.a12 * x + t.b12 * y + t.c12 < 0 &&
+                       t.a20 * x + t.b20 * y + t.c20 < 0;
+        q.push(c, lane, x - tx0, y - ty0, skey, a, tx0, ty0);
+        if (++x > lx1) {
+          x = lx0;
+          ++y;
         }
+      }
+      q.flush(skey, a, tx0, ty0);  // lane slots are rewritten by the next chunk
     }
+    __syncthreads();
+    const uint32_t nl = s_nlarge;
+    const bool more = s_next < hi;
+    // Phase 2: every warp walks the queued large triangles and takes an
+    // interleaved share of their 8x4 blocks (global block index mod warps).
+    int base = 0;
+    for (uint32_t k = 0; k < nl; ++k) {
+      const uint32_t rr = s_large[k];
+      const TriRaster tt = a.rast[rr];
+      const int bx0 = max((int)tt.bx0, tx0), bx1 = min((int)tt.bx1, tx1);
+      const int by0 = max((int)tt.by0, ty0), by1 = min((int)tt.by1, ty1);
+      const int nblk = ((bx1 - bx0 + 8) >> 3) * ((by1 - by0 + 4) >> 2);
+      const int j0 = (warp - base + kWarps) % kWarps;
+      const uint32_t slot = 32u + (k & 31u);
+      if ((k & 31u) == 0) q.flush(skey, a, tx0, ty0);  // slots 32..63 are about to be reused
+      if (lane == 0) {
+        tri[slot] = tt;
+        trec[slot] = rr;
+      }
+      __syncwarp();
+      walk_blocks<TS>(q, skey, a, tt, rr, slot, bx0, bx1, by0, by1, j0, kWarps, tx0, ty0);
+      base = (base + nblk) % kWarps;
+    }
+    q.flush(skey, a, tx0, ty0);
+    __syncthreads();
+    if (!more) break;
+    if (tid == 0) s_nlarge = 0;
+    __syncthreads();
   }
-  __syncthreads();
+
+  if (nslices > 1) {
+    // Merge this slice's keys into the tile's global keys; the last slice to
+    // arrive resolves the tile and returns the global keys to zero (zero is
+    // below every key, since no key encodes a NaN depth).
+    unsigned long long* g = a.gkey + (size_t)tile * (TS * TS);
+    for (int i = tid; i < TS * TS; i += kThreads) {
+      const unsigned long long k = skey[(i / TS) * kStride + (i % TS)];
+      if (k != BG_KEY) atomicMax(g + i, k);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&a.tile_done[tile], 1u) == nslices - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int i = tid; i < TS * TS; i += kThreads) {
+      const unsigned long long k = *(volatile unsigned long long*)(g + i);
+      skey[(i / TS) * kStride + (i % TS)] = k > BG_KEY ? k : BG_KEY;
+      g[i] = 0ull;
+    }
+    if (tid == 0) a.tile_done[tile] = 0u;
+    __syncthreads();
+  }
 
   // Resolve + deferred shading; Clear and DotGrid for uncovered pixels.
-  const int row = tid >> 3;
-  const int col = (tid & 7) << 2;
+  constexpr int kPerRow = TS / 4;
+  const int row = tid / kPerRow;
+  const int col = (tid % kPerRow) * 4;
   const int y = ty0 + row;
   if (y <= ty1) {
     uint32_t out_c[4];
     float out_z[4];
+    const ulonglong2* kp = reinterpret_cast<const ulonglong2*>(skey + row * kStride + col);
+    const ulonglong2 k01 = kp[0], k23 = kp[1];
+    const unsigned long long keys[4] = {k01.x, k01.y, k23.x, k23.y};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int x = tx0 + col + j;
-      const unsigned long long k = skey[row * kTileSize + col + j];
+      const unsigned long long k = keys[j];
       if (k == BG_KEY || x > tx1) {
         const bool dot = (x % 10 == 0) && (y % 10 == 0) && x >= 10 && y >= 10;  // DotGrid
         out_c[j] = dot ? 0xFF646464u : 0xFF323232u;
@@ -791,7 +1020,11 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     cudaEventRecord((cudaEvent_t)events[1], s);
     cudaEventRecord((cudaEvent_t)events[2], s);
   }
-  k_raster<<<a.tiles_x * a.tiles_y, kRasterThreads, 0, s>>>(a);
+  const int tiles = a.tiles_x * a.tiles_y;
+  if (a.tile_shift == 4)
+    k_raster<16><<<tiles * kRasterMaxSlices, RasterShape<16>::kThreads, 0, s>>>(a);
+  else
+    k_raster<32><<<tiles * kRasterMaxSlices, RasterShape<32>::kThreads, 0, s>>>(a);
   ++n;
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
   if (launches) *launches = n;

@@ -178,6 +178,14 @@ class Context:
     def flush_l2(self, nbytes: int = 512 << 20):
         N.check(N.lib().gr_context_flush_l2(self._h, nbytes))
 
+    def set_tuning(self, tile_size: int = 0, bin_capacity: int = 0):
+        N.check(N.lib().gr_context_set_tuning(self._h, tile_size, bin_capacity))
+
+    def tuning(self) -> Tuple[int, int]:
+        t, b = C.c_int32(), C.c_int32()
+        N.check(N.lib().gr_context_get_tuning(self._h, C.byref(t), C.byref(b)))
+        return int(t.value), int(b.value)
+
     def last_launches(self) -> int:
         n = C.c_int32()
         N.check(N.lib().gr_context_last_launches(self._h, C.byref(n)))

@@ -186,6 +186,11 @@ int32_t gr_context_event_elapsed(gr_context* ctx, int32_t start_slot, int32_t en
 /* Writes 'bytes' bytes of a scratch buffer on the context stream (flushes L2
  * between timed frames). */
 int32_t gr_context_flush_l2(gr_context* ctx, int64_t bytes);
+/* Raster tile size (16 or 32 pixels; 0 keeps the current one) and per-tile
+ * bin capacity in triangles (0 keeps the automatic size).  A frame whose
+ * bins overflow is re-run by gr_draw after the bins grow. */
+int32_t gr_context_set_tuning(gr_context* ctx, int32_t tile_size, int32_t bin_capacity);
+int32_t gr_context_get_tuning(gr_context* ctx, int32_t* tile_size, int32_t* bin_capacity);
 /* Number of kernels the last frame launched. */
 int32_t gr_context_last_launches(gr_context* ctx, int32_t* launches);
 /* Host<->device bytes the last gr_draw moved (draw items in; result words,

@@ -727,6 +727,26 @@ static void* raster_worker(void* arg) {
   return NULL;
 }
 
+int64_t orc_project(const orc_item* items, int32_t nitems, const orc_frame* fr, int64_t* xy_out,
+                    float* w_out, int64_t cap) {
+  int64_t n = 0;
+  for (int32_t i = 0; i < nitems; i++) {
+    TriList l = {0, 0, 0};
+    int e = project_object(&items[i], fr, &l);
+    if (e) { free(l.v); return e; }
+    for (int64_t k = 0; k < l.n; k++, n++) {
+      if (n >= cap) continue;
+      for (int j = 0; j < 3; j++) {
+        xy_out[6 * n + 2 * j] = l.v[k].x[j];
+        xy_out[6 * n + 2 * j + 1] = l.v[k].y[j];
+        w_out[3 * n + j] = l.v[k].w[j];
+      }
+    }
+    free(l.v);
+  }
+  return n;
+}
+
 int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr, uint8_t* rgba, float* z,
              int64_t* tpf, int32_t nthreads) {
   const int64_t npx = (int64_t)fr->width * fr->height;

@@ -93,6 +93,14 @@ typedef struct {
 int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr,
              uint8_t* rgba, float* z, int64_t* tpf, int32_t nthreads);
 
+/* Projection only: the binned triangles of every item in draw order, as
+ * drawProjection passes them to FrameBuffer.Triangle (int x, int y per
+ * vertex into xy_out, 6 per triangle; clip W into w_out, 3 per triangle).
+ * Returns the triangle count (entries beyond cap are counted, not written)
+ * or a negative error. */
+int64_t orc_project(const orc_item* items, int32_t nitems, const orc_frame* fr, int64_t* xy_out,
+                    float* w_out, int64_t cap);
+
 /* ---- per-stage entry points used by the known-answer tests ---- */
 
 /* matrixMultiplyVec4Batch (asm_amd64.s:7-50 / asm_purego.go:9-19), in place. */

@@ -67,6 +67,8 @@ def lib():
         L.orc_draw.argtypes = [C.POINTER(Item), C.c_int32, C.POINTER(Frame), C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_int64), C.c_int32]
         L.orc_draw.restype = C.c_int
+        L.orc_project.argtypes = [C.POINTER(Item), C.c_int32, C.POINTER(Frame), C.c_void_p, C.c_void_p, C.c_int64]
+        L.orc_project.restype = C.c_int64
         L.orc_transform_batch.argtypes = [fp, fp, C.c_int64]
         L.orc_facing_camera.argtypes = [fp, fp, fp]
         L.orc_facing_camera.restype = C.c_int
@@ -236,6 +238,55 @@ def make_texture(t, keep: _Keep) -> Texture:
     px = keep.arr(t.pixels, np.uint8)
     s.pixels = _ptr(px)
     return s
+
+
+def _setup(scene, flags, light, items_override, keep):
+    fov = fov_radians(scene.fov_deg)
+    meshes = {}
+    items = (Item * max(1, len(scene.objects)))()
+    for i, o in enumerate(scene.objects):
+        key = id(o.mesh)
+        if key not in meshes:
+            meshes[key] = make_mesh(o.mesh, keep)
+        items[i].mesh = C.pointer(meshes[key])
+        if items_override is not None:
+            mvp, w = items_override[i]
+        else:
+            mvp, w = object_matrices(o, scene.camera, scene.width, scene.height, fov)
+        for k in range(16):
+            items[i].mvp[k] = float(mvp[k])
+            items[i].world[k] = float(w[k])
+    keep.refs.append(meshes)
+    fr = Frame()
+    fr.width = scene.width
+    fr.height = scene.height
+    sm = screen_matrix(scene.width, scene.height)
+    for k in range(16):
+        fr.screen[k] = float(sm[k])
+    L = normalize3([-1.0, 1.0, 1.0]) if light is None else np.asarray(light, np.float32)
+    for k in range(3):
+        fr.light[k] = float(L[k])
+    fr.flags = scene.flags if flags is None else flags
+    texs = (Texture * max(1, len(scene.textures)))()
+    for i, t in enumerate(scene.textures):
+        texs[i] = make_texture(t, keep)
+    keep.refs.append(texs)
+    fr.textures = texs
+    fr.ntextures = len(scene.textures)
+    return items, fr
+
+
+def project_scene(scene, flags=None, light=None, items_override=None):
+    """Binned triangles of a scene: (xy int64 (n,3,2), w float32 (n,3))."""
+    keep = _Keep()
+    items, fr = _setup(scene, flags, light, items_override, keep)
+    cap = 8 * max(1, scene.num_triangles)
+    xy = np.zeros((cap, 3, 2), np.int64)
+    w = np.zeros((cap, 3), np.float32)
+    n = lib().orc_project(items, len(scene.objects), C.byref(fr), xy.ctypes.data, w.ctypes.data, cap)
+    if n < 0:
+        raise RuntimeError(f"orc_project failed: {n}")
+    return xy[:n], w[:n]
 
 
 def draw_scene(scene, nthreads: int = 1, flags: Optional[int] = None, light=None,
