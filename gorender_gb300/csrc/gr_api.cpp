@@ -92,6 +92,10 @@ struct gr_context {
   unsigned long long* gkey = nullptr;  // merged keys of tiles split over several CTAs
   uint32_t* tile_done = nullptr;
   uint32_t gkey_tiles = 0;
+  uint2* clip = nullptr;            // faces for the general clipper
+  uint32_t clip_cap = 0;
+  float* vlight = nullptr;          // per-normal Gouraud intensities
+  uint64_t vlight_cap = 0;
   uint32_t slice_entries = kDefaultSliceEntries;
   DevWork* work = nullptr;
   DevResult* d_result = nullptr;
@@ -107,7 +111,7 @@ struct gr_context {
   int last_launches = 0;
   int32_t pending = GR_OK;
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes of the last draw
-  uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0;
+  uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0, want_clip_cap = 0;
   int tile_shift = kDefaultTileShift;  // raster tile size (autotuned per workload)
 };
 
@@ -224,6 +228,14 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
     c->tiles_cap = nt;
     c->bin_cap = nc;
   }
+  uint64_t want_clip = std::max<uint64_t>(c->want_clip_cap, faces / 16 + 1024);
+  if (want_clip > c->clip_cap) {
+    if ((st = sync())) return st;
+    dev_free(c->clip);
+    c->clip_cap = 0;
+    if ((st = dev_alloc(&c->clip, want_clip))) return st;
+    c->clip_cap = (uint32_t)want_clip;
+  }
   uint64_t want_big = std::max<uint64_t>(c->want_big_cap, faces / 8 + 1024);
   if (want_big > c->big_cap) {
     if ((st = sync())) return st;
@@ -288,6 +300,8 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   const bool gouraud = (p->flags & GR_LIGHTING) && !(p->flags & GR_FLAT_SHADING);
   uint64_t faces = 0;
   int blocks = 0;
+  int light_blocks = 0;
+  uint64_t light_total = 0;
   int live = 0;
   for (int i = 0; i < n; ++i) {
     int m = items[i].mesh;
@@ -309,12 +323,27 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
     d.face_base = (uint32_t)fb;
     d.block_base = blocks;
     blocks += (mr.nf + kProjectThreads - 1) / kProjectThreads;
+    // every item gets a k_light block range (empty for non-Gouraud items) so the
+    // kernel's block -> item search sees non-decreasing bases
+    d.light_base = (int)light_total;
+    d.light_block_base = light_blocks;
+    if (gouraud && mr.nn > 0) {
+      light_total += (uint64_t)mr.nn;
+      light_blocks += (mr.nn + 255) / 256;
+    }
   }
   if (faces >= (1ull << 28)) return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces in one frame");
   const int ts = 1 << c->tile_shift;
   const int tiles_x = (p->width + ts - 1) / ts;
   const int tiles_y = (p->height + ts - 1) / ts;
   if ((st = ensure_frame_buffers(c, faces, (uint32_t)(tiles_x * tiles_y)))) return st;
+  if (light_total > c->vlight_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->vlight);
+    c->vlight_cap = 0;
+    if ((st = dev_alloc(&c->vlight, light_total))) return st;
+    c->vlight_cap = light_total;
+  }
   if (live) CK(cudaMemcpyAsync(c->d_items, c->h_items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
   c->h2d_bytes = (int64_t)sizeof(DevItem) * live;
   c->d2h_bytes = 0;
@@ -349,6 +378,10 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   a.gkey = c->gkey;
   a.tile_done = c->tile_done;
   a.slice_entries = c->slice_entries;
+  a.clip = c->clip;
+  a.clip_cap = c->clip_cap;
+  a.vlight = c->vlight;
+  a.light_blocks = light_blocks;
   a.work = c->work;
   a.result = c->d_result;
   out.faces = faces;
@@ -377,6 +410,7 @@ int check_result(gr_context* c, const DevResult& r, int32_t* err) {
   if (r.bin_need > c->bin_cap) { c->want_bin_cap = next_pow2((uint64_t)r.bin_need + r.bin_need / 4); rerun = 1; }
   if (r.rec_need > c->rec_cap) { c->want_rec_cap = r.rec_need + r.rec_need / 8; rerun = 1; }
   if (r.big_need > c->big_cap) { c->want_big_cap = next_pow2((uint64_t)r.big_need + r.big_need / 4); rerun = 1; }
+  if (r.clip_need > c->clip_cap) { c->want_clip_cap = next_pow2((uint64_t)r.clip_need + r.clip_need / 4); rerun = 1; }
   if (r.error & 1u) *err = fail(GR_ERR_CLIP_OVERFLOW, "a clipped polygon exceeded 9 vertices");
   return rerun;
 }
@@ -468,7 +502,7 @@ int32_t gr_context_destroy(gr_context* c) {
   if (c->h_items) cudaFreeHost(c->h_items);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->big);
-  dev_free(c->gkey); dev_free(c->tile_done);
+  dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
   dev_free(c->work); dev_free(c->d_result);
   if (c->h_result) cudaFreeHost(c->h_result);
   dev_free(c->fb_rgba); dev_free(c->fb_z);

@@ -5,6 +5,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace gr {
 
 constexpr int kDefaultTileShift = 5;          // 32 x 32 pixel raster tiles (16 x 16: shift 4)
@@ -16,6 +18,7 @@ constexpr int kProjectThreads = 256;
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
 constexpr int kRasterMaxSlices = 8;           // CTAs that may share one tile's bin
 constexpr int kDefaultSliceEntries = 128;     // bin entries per slice before a tile is split
+constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 
 // Texture table entry (texture.go:19-26).
 struct DevTex {
@@ -41,8 +44,10 @@ struct DevItem {
   const float* vcol;                // nv x 3 (may be null)
   int nv, nn, nf;
   uint32_t face_base;               // global face order of face 0
-  int block_base;                   // first project block of this item
-  int pad[3];
+  int block_base;                   // first k_project block of this item
+  int light_base;                   // first entry of this item in FrameArgs::vlight
+  int light_block_base;             // first k_light block of this item
+  int pad;
 };
 
 // Raster setup of one binned triangle (64 bytes).  For "narrow" triangles
@@ -88,11 +93,13 @@ struct DevWork {
   unsigned int rec_need;            // records needed when over capacity
   unsigned int big_need;
   unsigned int error;               // bit 0 clip overflow, bit 1 bad normal index
+  unsigned int nclip;               // faces queued for the general clipper
+  unsigned int clip_need;
 };
 
 struct DevResult {
   unsigned long long tpf;
-  unsigned int nrec, nbig, bin_need, rec_need, big_need, error;
+  unsigned int nrec, nbig, bin_need, rec_need, big_need, error, nclip, clip_need;
 };
 
 // Everything a frame's kernels need, passed by value.
@@ -121,6 +128,10 @@ struct FrameArgs {
   uint32_t* bins;                   // tiles x bin_cap record indices
   uint32_t* bin_count;              // per tile
   uint32_t* big;                    // multi-tile record queue
+  uint2* clip;                      // (item, face) pairs for the general clipper
+  uint32_t clip_cap;
+  float* vlight;                    // per-normal Gouraud intensities (k_light)
+  int light_blocks;                 // k_light grid (0: no Gouraud item)
   unsigned long long* gkey;         // tiles x 1024 merged visibility keys of split tiles (zero when idle)
   uint32_t* tile_done;              // per tile: slices finished (zero when idle)
   uint32_t slice_entries;           // bin entries per slice

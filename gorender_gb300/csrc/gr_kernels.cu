@@ -287,8 +287,153 @@ __device__ __forceinline__ void bin_store(const FrameArgs& a, uint32_t tile, uin
     atomicMax(&a.work->bin_need, pos + 1);
 }
 
+// Lighting of one normal (renderer.go:326-346): 0.5 + (normalize(W*n) . L) * 0.5
+// with Vec4.Normalize, whose length includes w.
+__device__ __forceinline__ float light_of(const float* world, V4 nrm, const float* L) {
+  V4 n = mat_vec(world, nrm);
+  float len = __fsqrt_rn(fa(fa(fa(fm(n.x, n.x), fm(n.y, n.y)), fm(n.z, n.z)), fm(n.w, n.w)));
+  float x = fd(n.x, len), y = fd(n.y, len), z = fd(n.z, len);
+  float d = fa(fa(fm(x, L[0]), fm(y, L[1])), fm(z, L[2]));
+  return fa(0.5f, fm(d, 0.5f));
+}
+
+__device__ __forceinline__ bool gouraud(const FrameArgs& a, const DevItem& it) {
+  return (a.flags & 0x08u) && !(a.flags & 0x10u) && it.nn != 0;
+}
+
+// facingCamera (renderer.go:246-250) on clip-space vertices.
+__device__ __forceinline__ bool facing_camera(V4 v0, V4 v1, V4 v2) {
+  float e1x = fs(v1.x, v0.x), e1y = fs(v1.y, v0.y), e1z = fs(v1.z, v0.z);
+  float e2x = fs(v2.x, v0.x), e2y = fs(v2.y, v0.y), e2z = fs(v2.z, v0.z);
+  float nx = fs(fm(e1y, e2z), fm(e1z, e2y));
+  float ny = fs(fm(e1z, e2x), fm(e1x, e2z));
+  float nz = fs(fm(e1x, e2y), fm(e1y, e2x));
+  float d = fa(fa(fm(nx, fs(0.0f, v0.x)), fm(ny, fs(0.0f, v0.y))), fm(nz, fs(0.0f, v0.z)));
+  return d > 0.0f;
+}
+
+// Per-vertex attributes of face f (intensity, UV, RGB) and its texture slot.
+__device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevItem& it, int f, int i0, int i1, int i2,
+                                                const float* world, PV& p0, PV& p1, PV& p2, int& tex) {
+  const uint32_t fl = a.flags;
+  float in0, in1, in2;
+  if (fl & 0x08u) {
+    if (gouraud(a, it)) {
+      // per-normal intensities computed once per frame by k_light
+      const float* vl = a.vlight + it.light_base;
+      in0 = __ldg(vl + __ldg(it.nidx + 3 * f));
+      in1 = __ldg(vl + __ldg(it.nidx + 3 * f + 1));
+      in2 = __ldg(vl + __ldg(it.nidx + 3 * f + 2));
+    } else {
+      in0 = in1 = in2 = light_of(world, ld4(it.fnrm + 4 * (size_t)f), a.L);
+    }
+  } else {
+    in0 = in1 = in2 = 0.5f;
+  }
+  p0.in = in0; p1.in = in1; p2.in = in2;
+  if (it.uv) {
+    const float2* uv = reinterpret_cast<const float2*>(it.uv + 6 * (size_t)f);
+    const float2 t0 = __ldg(uv), t1 = __ldg(uv + 1), t2 = __ldg(uv + 2);
+    p0.u = t0.x; p0.v = t0.y; p1.u = t1.x; p1.v = t1.y; p2.u = t2.x; p2.v = t2.y;
+  } else {
+    p0.u = p0.v = p1.u = p1.v = p2.u = p2.v = 0.0f;
+  }
+  if (it.vcol) {
+    const float* c0 = it.vcol + 3 * (size_t)i0;
+    const float* c1 = it.vcol + 3 * (size_t)i1;
+    const float* c2 = it.vcol + 3 * (size_t)i2;
+    p0.r = __ldg(c0); p0.g = __ldg(c0 + 1); p0.b = __ldg(c0 + 2);
+    p1.r = __ldg(c1); p1.g = __ldg(c1 + 1); p1.b = __ldg(c1 + 2);
+    p2.r = __ldg(c2); p2.g = __ldg(c2 + 1); p2.b = __ldg(c2 + 2);
+  } else {
+    p0.r = p0.g = p0.b = p1.r = p1.g = p1.b = p2.r = p2.g = p2.b = 0.0f;
+  }
+  const int t = it.tex ? __ldg(it.tex + f) : -1;
+  tex = ((fl & 0x20u) && t >= 0) ? t : (it.vcol ? -2 : -1);  // renderer.go:176-178
+}
+
+// Writes record r of a set-up triangle (raster part, int64 edges, shading).
+__device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Setup& s, const SV& q0, const SV& q1,
+                                             const SV& q2, int tex, uint32_t okey) {
+  s.r.key = okey | (s.wide ? 0x80000000u : 0u);
+  const int4* src = reinterpret_cast<const int4*>(&s.r);
+  int4* dst = reinterpret_cast<int4*>(a.rast + r);
+  dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
+  if (s.wide) {
+    const int4* ws = reinterpret_cast<const int4*>(&s.w);
+    int4* wd = reinterpret_cast<int4*>(a.wide + r);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) wd[q] = ws[q];
+  }
+  TriShade sh;
+  sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);  // rasterizer.go:132-137
+  sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
+  sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
+  sh.i0 = q0.in; sh.i1 = q1.in; sh.i2 = q2.in;
+  sh.tex = tex;
+  sh.pad[0] = sh.pad[1] = 0.0f;
+  const float4* ss = reinterpret_cast<const float4*>(&sh);
+  float4* sd = reinterpret_cast<float4*>(a.shade + r);
+  sd[0] = ss[0]; sd[1] = ss[1]; sd[2] = ss[2];
+  if (tex == -2) {
+    TriColor* c = a.tcol + r;
+    c->c[0] = q0.r; c->c[1] = q0.g; c->c[2] = q0.b;
+    c->c[3] = q1.r; c->c[4] = q1.g; c->c[5] = q1.b;
+    c->c[6] = q2.r; c->c[7] = q2.g; c->c[8] = q2.b;
+  }
+  if (okey < a.key_cap) a.rec_of_key[okey] = r;
+}
+
+// Binning without warp aggregation (the rare clipped path).
+__device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const TriRaster& t) {
+  const uint32_t tx0 = (uint32_t)t.bx0 >> a.tile_shift, tx1 = (uint32_t)t.bx1 >> a.tile_shift;
+  const uint32_t ty0 = (uint32_t)t.by0 >> a.tile_shift, ty1 = (uint32_t)t.by1 >> a.tile_shift;
+  const uint32_t ntiles = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+  if (ntiles <= (uint32_t)kBinDirectMax) {
+    for (uint32_t ty = ty0; ty <= ty1; ++ty)
+      for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+        const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
+        bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+      }
+  } else {
+    const uint32_t q = atomicAdd(&a.work->nbig, 1u);
+    if (q < a.big_cap) a.big[q] = r;
+    else atomicMax(&a.work->big_need, q + 1);
+  }
+}
+
+// Block -> item: the last item whose first block is <= blockIdx.x.
+__device__ __forceinline__ int find_item(const FrameArgs& a, bool light_blocks) {
+  int lo = 0, hi = a.num_items - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    int base = light_blocks ? a.items[mid].light_block_base : a.items[mid].block_base;
+    if (base <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---------------------------------------------------------------------------
-// k_project
+// k_light: Gouraud intensity of every vertex normal of every item, once per
+// frame.  The reference normalises WorldVertexNormals[NormalIndices[k]] per
+// face corner (renderer.go:327-333); the value depends only on the normal
+// index, so computing it once per normal gives the same bits.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
+  __shared__ float s_world[16];
+  __shared__ int s_item;
+  if (threadIdx.x == 0) s_item = find_item(a, true);
+  __syncthreads();
+  const DevItem& it = a.items[s_item];
+  if (threadIdx.x < 16) s_world[threadIdx.x] = it.world[threadIdx.x];
+  __syncthreads();
+  if (!gouraud(a, it)) return;
+  const int n = ((int)blockIdx.x - it.light_block_base) * 256 + (int)threadIdx.x;
+  if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.L);
+}
+
+// ---------------------------------------------------------------------------
+// k_project: one thread per face; everything but the general clipper.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) {
   __shared__ float s_mvp[16];
@@ -298,16 +443,10 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   __shared__ unsigned s_out[8];
 
   const int tid = threadIdx.x;
-  if (tid == 0) {
-    int lo = 0, hi = a.num_items - 1;
-    while (lo < hi) {  // last item with block_base <= blockIdx.x
-      int mid = (lo + hi + 1) >> 1;
-      if (a.items[mid].block_base <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
-    }
-    s_item = lo;
-  }
+  if (tid == 0) s_item = find_item(a, false);
   __syncthreads();
-  const DevItem& it = a.items[s_item];
+  const int item = s_item;
+  const DevItem& it = a.items[item];
   if (tid < 16) {
     s_mvp[tid] = it.mvp[tid];
     s_world[tid] = it.world[tid];
@@ -343,237 +482,251 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   const bool valid = f < it.nf;
   const unsigned lane = lane_id();
 
-  // mode 0: nothing to draw; 1: the face itself (registers only);
-  // 2: a clipped polygon (local memory, rare)
-  int mode = 0;
-  int pcount = 0;
+  bool emit = false;   // this face yields one record
+  bool general = false;  // this face needs the general clipper (k_clip)
+  int ntpf = 0;
   int tex = -1;
-  PV p0, p1, p2;
-  PV poly[9];
+  SV s0, s1, s2;
   if (valid) {
     const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
-    V4 v0 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i0));
-    V4 v1 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i1));
-    V4 v2 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i2));
-    bool draw = true;
-    if (fl & 0x04u) {  // BackfaceCulling: facingCamera (renderer.go:246-250)
-      float e1x = fs(v1.x, v0.x), e1y = fs(v1.y, v0.y), e1z = fs(v1.z, v0.z);
-      float e2x = fs(v2.x, v0.x), e2y = fs(v2.y, v0.y), e2z = fs(v2.z, v0.z);
-      float nx = fs(fm(e1y, e2z), fm(e1z, e2y));
-      float ny = fs(fm(e1z, e2x), fm(e1x, e2z));
-      float nz = fs(fm(e1x, e2y), fm(e1y, e2x));
-      float d = fa(fa(fm(nx, fs(0.0f, v0.x)), fm(ny, fs(0.0f, v0.y))), fm(nz, fs(0.0f, v0.z)));
-      draw = d > 0.0f;
-    }
+    const V4 v0 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i0));
+    const V4 v1 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i1));
+    const V4 v2 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i2));
+    bool draw = !(fl & 0x04u) || facing_camera(v0, v1, v2);  // BackfaceCulling
     // Frustum clipping (renderer.go:349-359).  At the first plane, in clipping
     // order, where not all three vertices are inside: all outside means the
     // polygon reaching that plane is still the face itself (every earlier pass
     // only rotated it), so ClipTriangle returns no triangle; a mix needs the
     // general clipper.  With no such plane the six passes rotate the face back
     // to itself and it passes through unchanged.
-    int clip = 0;  // 0 pass through, 1 rejected, 2 general
     if (draw && (fl & 0x01u) && vis != 2) {
       for (int i = 0; i < 6; ++i) {
         const int m = (int)plane_inside(i, v0) + (int)plane_inside(i, v1) + (int)plane_inside(i, v2);
         if (m == 3) continue;
-        clip = (m == 0) ? 1 : 2;
+        if (m == 0) draw = false;
+        else general = true;
         break;
       }
     }
-    if (draw && clip != 1) {
-      float in0, in1, in2;
-      if (fl & 0x08u) {  // Lighting (renderer.go:326-346)
-        if (it.nn != 0 && !(fl & 0x10u)) {
-          float in[3];
-          for (int k = 0; k < 3; ++k) {
-            int ni = __ldg(it.nidx + 3 * f + k);
-            V4 n = mat_vec(s_world, ld4(it.vnrm + 4 * (size_t)ni));
-            float len = __fsqrt_rn(fa(fa(fa(fm(n.x, n.x), fm(n.y, n.y)), fm(n.z, n.z)), fm(n.w, n.w)));
-            float x = fd(n.x, len), y = fd(n.y, len), z = fd(n.z, len);
-            float d = fa(fa(fm(x, a.L[0]), fm(y, a.L[1])), fm(z, a.L[2]));
-            in[k] = fa(0.5f, fm(d, 0.5f));
-          }
-          in0 = in[0]; in1 = in[1]; in2 = in[2];
-        } else {
-          V4 n = mat_vec(s_world, ld4(it.fnrm + 4 * (size_t)f));
-          float len = __fsqrt_rn(fa(fa(fa(fm(n.x, n.x), fm(n.y, n.y)), fm(n.z, n.z)), fm(n.w, n.w)));
-          float x = fd(n.x, len), y = fd(n.y, len), z = fd(n.z, len);
-          float d = fa(fa(fm(x, a.L[0]), fm(y, a.L[1])), fm(z, a.L[2]));
-          in0 = in1 = in2 = fa(0.5f, fm(d, 0.5f));
-        }
-      } else {
-        in0 = in1 = in2 = 0.5f;
-      }
+    if (draw && !general) {
+      PV p0, p1, p2;
       p0.p = v0; p1.p = v1; p2.p = v2;
-      p0.in = in0; p1.in = in1; p2.in = in2;
-      if (it.uv) {
-        const float2* uv = reinterpret_cast<const float2*>(it.uv + 6 * (size_t)f);
-        const float2 t0 = __ldg(uv), t1 = __ldg(uv + 1), t2 = __ldg(uv + 2);
-        p0.u = t0.x; p0.v = t0.y; p1.u = t1.x; p1.v = t1.y; p2.u = t2.x; p2.v = t2.y;
-      } else {
-        p0.u = p0.v = p1.u = p1.v = p2.u = p2.v = 0.0f;
-      }
-      if (it.vcol) {
-        const float* c0 = it.vcol + 3 * (size_t)i0;
-        const float* c1 = it.vcol + 3 * (size_t)i1;
-        const float* c2 = it.vcol + 3 * (size_t)i2;
-        p0.r = __ldg(c0); p0.g = __ldg(c0 + 1); p0.b = __ldg(c0 + 2);
-        p1.r = __ldg(c1); p1.g = __ldg(c1 + 1); p1.b = __ldg(c1 + 2);
-        p2.r = __ldg(c2); p2.g = __ldg(c2 + 1); p2.b = __ldg(c2 + 2);
-      } else {
-        p0.r = p0.g = p0.b = p1.r = p1.g = p1.b = p2.r = p2.g = p2.b = 0.0f;
-      }
-      int t = it.tex ? __ldg(it.tex + f) : -1;
-      tex = ((fl & 0x20u) && t >= 0) ? t : (it.vcol ? -2 : -1);  // renderer.go:176-178
-      mode = 1;
-      if (clip == 2) {
-        PV tmp[9];
-        poly[0] = p0; poly[1] = p1; poly[2] = p2;
-        pcount = clip_polygon(poly, tmp);
-        if (pcount < 0) {
-          atomicOr(&a.work->error, 1u);
-          pcount = 0;
-        }
-        mode = pcount >= 3 ? 2 : 0;
+      face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
+      s0 = to_screen(p0, a.S);
+      s1 = to_screen(p1, a.S);
+      s2 = to_screen(p2, a.S);
+      if (bin_test(s0, s1, s2, (float)a.W, (float)a.H)) {
+        ntpf = 1;
+        Setup s;
+        // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
+        emit = (fl & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s);
       }
     }
   }
 
-  // Divide + screen map per polygon vertex, bin test and setup per fan triangle.
-  SV s0, s1, s2;
-  SV sv[9];
-  unsigned fanmask = 0;
-  int ntpf = 0;
-  const float Wf = (float)a.W, Hf = (float)a.H;
-  if (mode == 1) {
-    s0 = to_screen(p0, a.S);
-    s1 = to_screen(p1, a.S);
-    s2 = to_screen(p2, a.S);
-    if (bin_test(s0, s1, s2, Wf, Hf)) {
-      ntpf = 1;
-      Setup s;
-      // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
-      if ((fl & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s)) fanmask = 1u;
-    }
-  } else if (mode == 2) {
-    for (int k = 0; k < pcount; ++k) sv[k] = to_screen(poly[k], a.S);
-    for (int t = 0; t + 2 < pcount; ++t) {
-      if (!bin_test(sv[0], sv[t + 1], sv[t + 2], Wf, Hf)) continue;
-      ++ntpf;
-      Setup s;
-      if ((fl & 0x02u) && setup_tri(sv[0], sv[t + 1], sv[t + 2], a.W, a.H, s)) fanmask |= 1u << t;
+  // Faces for the general clipper: one atomic per warp.
+  const unsigned gm = __ballot_sync(FULL_MASK, general);
+  if (gm) {
+    uint32_t qb = 0;
+    const int ldr = __ffs(gm) - 1;
+    if ((int)lane == ldr) qb = atomicAdd(&a.work->nclip, (uint32_t)__popc(gm));
+    qb = __shfl_sync(FULL_MASK, qb, ldr);
+    if (general) {
+      const uint32_t q = qb + __popc(gm & ((1u << lane) - 1u));
+      if (q < a.clip_cap) a.clip[q] = make_uint2((uint32_t)item, (uint32_t)f);
+      else atomicMax(&a.work->clip_need, q + 1);
     }
   }
 
   // TPF: one atomic per warp.
-  int wt = __reduce_add_sync(FULL_MASK, ntpf);
+  const int wt = __reduce_add_sync(FULL_MASK, ntpf);
   if (lane == 0 && wt) atomicAdd(&a.work->tpf, (unsigned long long)wt);
 
-  // Compact records: warp exclusive scan of per-lane counts, one atomic per warp.
-  const int nmine = __popc(fanmask);
-  int incl = nmine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL_MASK, incl, o);
-    if ((int)lane >= o) incl += y;
+  // Compact records: one atomic per warp, lane offsets from the ballot.
+  const unsigned em = __ballot_sync(FULL_MASK, emit);
+  if (em == 0) return;
+  uint32_t base = 0;
+  const int ldr = __ffs(em) - 1;
+  if ((int)lane == ldr) {
+    base = atomicAdd(&a.work->nrec, (uint32_t)__popc(em));
+    if (base + (uint32_t)__popc(em) > a.rec_cap) atomicMax(&a.work->rec_need, base + (uint32_t)__popc(em));
   }
-  const int total = __shfl_sync(FULL_MASK, incl, 31);
-  if (total == 0) return;
-  unsigned base = 0;
-  if (lane == 31) base = atomicAdd(&a.work->nrec, (unsigned)total);
-  base = __shfl_sync(FULL_MASK, base, 31);
-  if (lane == 31 && base + (unsigned)total > a.rec_cap) atomicMax(&a.work->rec_need, base + (unsigned)total);
-  unsigned my = base + (unsigned)(incl - nmine);
-  const int maxn = __reduce_max_sync(FULL_MASK, nmine);
-  const uint32_t face_key = (it.face_base + (uint32_t)(valid ? f : 0)) * (uint32_t)kKeysPerFace;
+  base = __shfl_sync(FULL_MASK, base, ldr);
+  const uint32_t r = base + __popc(em & ((1u << lane) - 1u));
+  const bool ok = emit && r < a.rec_cap;
+  uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
+  if (ok) {
+    Setup s;
+    setup_tri(s0, s1, s2, a.W, a.H, s);
+    write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
+    tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
+    tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
+    ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
+    ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
+  }
+  const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
+  // single-tile triangles: warp-aggregated append per distinct tile
+  const bool one = ntiles == 1;
+  const unsigned m1 = __ballot_sync(FULL_MASK, one);
+  if (one) {
+    const uint32_t tile = ty0 * (uint32_t)a.tiles_x + tx0;
+    const unsigned grp = __match_any_sync(m1, tile);
+    const int leader = __ffs(grp) - 1;
+    const unsigned rank = __popc(grp & ((1u << lane) - 1u));
+    uint32_t pos = 0;
+    if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
+    pos = __shfl_sync(grp, pos, leader) + rank;
+    bin_store(a, tile, pos, r);
+  }
+  // two to four tiles: direct appends
+  if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
+    for (uint32_t ty = ty0; ty <= ty1; ++ty)
+      for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+        const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
+        bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+      }
+  }
+  // more: the multi-tile queue, one atomic per warp
+  const bool many = ntiles > (uint32_t)kBinDirectMax;
+  const unsigned mm = __ballot_sync(FULL_MASK, many);
+  if (mm) {
+    uint32_t qb = 0;
+    const int l2 = __ffs(mm) - 1;
+    if ((int)lane == l2) qb = atomicAdd(&a.work->nbig, (uint32_t)__popc(mm));
+    qb = __shfl_sync(FULL_MASK, qb, l2);
+    if (many) {
+      const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
+      if (q < a.big_cap) a.big[q] = r;
+      else atomicMax(&a.work->big_need, q + 1);
+    }
+  }
+}
 
-  unsigned rem = fanmask;
-  for (int iter = 0; iter < maxn; ++iter) {
-    bool has = rem != 0;
-    int t = has ? __ffs(rem) - 1 : 0;
-    if (has) rem &= rem - 1;
-    uint32_t r = my;
-    bool ok = has && r < a.rec_cap;
-    if (has) ++my;
-    uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
-    if (ok) {
-      SV q0 = s0, q1 = s1, q2 = s2;
-      if (mode == 2) {
-        q0 = sv[0];
-        q1 = sv[t + 1];
-        q2 = sv[t + 2];
-      }
-      Setup s;
-      setup_tri(q0, q1, q2, a.W, a.H, s);
-      uint32_t okey = face_key + (uint32_t)t + 1u;
-      s.r.key = okey | (s.wide ? 0x80000000u : 0u);
-      const int4* src = reinterpret_cast<const int4*>(&s.r);
-      int4* dst = reinterpret_cast<int4*>(a.rast + r);
-      dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-      if (s.wide) {
-        const int4* ws = reinterpret_cast<const int4*>(&s.w);
-        int4* wd = reinterpret_cast<int4*>(a.wide + r);
+// ---------------------------------------------------------------------------
+// k_clip: faces that straddle a frustum plane, one warp per face.  The
+// polygon lives in registers, vertex k on lane k.  Each plane pass of
+// Frustum.ClipTriangle (clipping.go:199-232) visits edges b = 0..count-1 with
+// A = vertex b+1, B = vertex b and emits (I, A), (A), (I) or nothing; here lane
+// b computes its edge's outputs, a warp scan of the output counts gives their
+// positions in the reference's order, and every output lane gathers its
+// vertex with shuffles.  Fan triangles (clipping.go:42-62) go one per lane.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ PV shfl_pv(const PV& v, int src) {
+  PV o;
+  o.p.x = __shfl_sync(FULL_MASK, v.p.x, src);
+  o.p.y = __shfl_sync(FULL_MASK, v.p.y, src);
+  o.p.z = __shfl_sync(FULL_MASK, v.p.z, src);
+  o.p.w = __shfl_sync(FULL_MASK, v.p.w, src);
+  o.u = __shfl_sync(FULL_MASK, v.u, src);
+  o.v = __shfl_sync(FULL_MASK, v.v, src);
+  o.in = __shfl_sync(FULL_MASK, v.in, src);
+  o.r = __shfl_sync(FULL_MASK, v.r, src);
+  o.g = __shfl_sync(FULL_MASK, v.g, src);
+  o.b = __shfl_sync(FULL_MASK, v.b, src);
+  return o;
+}
+
+__device__ __forceinline__ SV shfl_sv(const SV& v, int src) {
+  SV o;
+  o.X = __shfl_sync(FULL_MASK, v.X, src);
+  o.Y = __shfl_sync(FULL_MASK, v.Y, src);
+  o.sx = __shfl_sync(FULL_MASK, v.sx, src);
+  o.sy = __shfl_sync(FULL_MASK, v.sy, src);
+  o.W = __shfl_sync(FULL_MASK, v.W, src);
+  o.u = __shfl_sync(FULL_MASK, v.u, src);
+  o.v = __shfl_sync(FULL_MASK, v.v, src);
+  o.in = __shfl_sync(FULL_MASK, v.in, src);
+  o.r = __shfl_sync(FULL_MASK, v.r, src);
+  o.g = __shfl_sync(FULL_MASK, v.g, src);
+  o.b = __shfl_sync(FULL_MASK, v.b, src);
+  return o;
+}
+
+__global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
+  const uint32_t nclip = min(*(volatile uint32_t*)&a.work->nclip, a.clip_cap);
+  const int lane = (int)lane_id();
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nclip; q += warps) {
+    const uint2 e = a.clip[q];
+    const DevItem& it = a.items[e.x];
+    const int f = (int)e.y;
+    // lanes 0..2: the face's vertices with their attributes
+    PV v;
+    int tex = -1;
+    {
+      const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
+      PV p0, p1, p2;
+      face_attributes(a, it, f, i0, i1, i2, it.world, p0, p1, p2, tex);
+      const int ik = lane == 0 ? i0 : (lane == 1 ? i1 : i2);
+      v = lane == 0 ? p0 : (lane == 1 ? p1 : p2);
+      v.p = mat_vec(it.mvp, ld4(it.pos + 4 * (size_t)ik));
+    }
+    int count = 3;
+    bool overflow = false;
+    for (int pi = 0; pi < 6 && count > 0; ++pi) {
+      const bool act = lane < count;
+      const PV A = shfl_pv(v, (lane + 1 < count) ? lane + 1 : 0);  // a = (b+1) % count
+      const bool inA = act && plane_inside(pi, A.p);
+      const bool inB = act && plane_inside(pi, v.p);
+      const int nout = inA ? (inB ? 1 : 2) : (inB ? 1 : 0);
+      PV X = A;
+      if (inA != inB) X = intersect(pi, A, v);
+      // exclusive scan of the output counts in edge order
+      int incl = nout;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) wd[q] = ws[q];
+      for (int o = 1; o < 16; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= o) incl += y;
       }
-      TriShade sh;
-      sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);
-      sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
-      sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
-      sh.i0 = q0.in; sh.i1 = q1.in; sh.i2 = q2.in;
-      sh.tex = tex;
-      sh.pad[0] = sh.pad[1] = 0.0f;
-      const float4* ss = reinterpret_cast<const float4*>(&sh);
-      float4* sd = reinterpret_cast<float4*>(a.shade + r);
-      sd[0] = ss[0]; sd[1] = ss[1]; sd[2] = ss[2];
-      if (tex == -2) {
-        TriColor* c = a.tcol + r;
-        c->c[0] = q0.r; c->c[1] = q0.g; c->c[2] = q0.b;
-        c->c[3] = q1.r; c->c[4] = q1.g; c->c[5] = q1.b;
-        c->c[6] = q2.r; c->c[7] = q2.g; c->c[8] = q2.b;
+      const int total = __shfl_sync(FULL_MASK, incl, 15);
+      const int pos = incl - nout;
+      if (total > 9) {  // the reference would index past its 9-vertex arrays
+        overflow = true;
+        break;
       }
-      if (okey < a.key_cap) a.rec_of_key[okey] = r;
-      tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
-      tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
-      ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
-      ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
+      // output j comes from the last edge lane whose range starts at or before j
+      int src = 0;
+      for (int l = 0; l < 9; ++l) {
+        const int pl = __shfl_sync(FULL_MASK, pos, l);
+        const int nl = __shfl_sync(FULL_MASK, nout, l);
+        if (nl > 0 && pl <= lane) src = l;
+      }
+      const int spos = __shfl_sync(FULL_MASK, pos, src);
+      const int sn = __shfl_sync(FULL_MASK, nout, src);
+      const PV gX = shfl_pv(X, src);
+      const PV gA = shfl_pv(A, src);
+      // a two-output edge emits (I, A); a one-output edge emits A when A is
+      // inside, else I
+      const int src_in_a = __shfl_sync(FULL_MASK, (int)inA, src);  // every lane shuffles
+      const bool takeX = (sn == 2) ? (lane == spos) : !src_in_a;
+      if (lane < total) v = takeX ? gX : gA;
+      count = total;
     }
-    const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
-    // single-tile triangles: warp-aggregated append per distinct tile
-    const bool one = ntiles == 1;
-    const unsigned m1 = __ballot_sync(FULL_MASK, one);
-    if (one) {
-      const uint32_t tile = ty0 * (uint32_t)a.tiles_x + tx0;
-      const unsigned grp = __match_any_sync(m1, tile);
-      const int leader = __ffs(grp) - 1;
-      const unsigned rank = __popc(grp & ((1u << lane) - 1u));
-      uint32_t pos = 0;
-      if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
-      pos = __shfl_sync(grp, pos, leader) + rank;
-      bin_store(a, tile, pos, r);
+    if (overflow) {
+      if (lane == 0) atomicOr(&a.work->error, 1u);
+      continue;
     }
-    // two to four tiles: direct appends
-    if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
-      for (uint32_t ty = ty0; ty <= ty1; ++ty)
-        for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-          const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
-          bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+    if (count < 3) continue;  // Polygon.Triangulate returns nothing
+    const SV sv = to_screen(v, a.S);  // lane k: polygon vertex k
+    const SV s0 = shfl_sv(sv, 0), s1 = shfl_sv(sv, lane + 1 < 9 ? lane + 1 : 0),
+             s2 = shfl_sv(sv, lane + 2 < 9 ? lane + 2 : 0);
+    const bool fan = lane + 2 < count;
+    int ntpf = 0;
+    if (fan && bin_test(s0, s1, s2, (float)a.W, (float)a.H)) {
+      ntpf = 1;
+      Setup s;
+      if ((a.flags & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s)) {
+        const uint32_t r = atomicAdd(&a.work->nrec, 1u);
+        if (r < a.rec_cap) {
+          write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
+          bin_record(a, r, s.r);
+        } else {
+          atomicMax(&a.work->rec_need, r + 1);
         }
-    }
-    // more: the multi-tile queue, one atomic per warp
-    const bool many = ntiles > (uint32_t)kBinDirectMax;
-    const unsigned mm = __ballot_sync(FULL_MASK, many);
-    if (mm) {
-      uint32_t qb = 0;
-      const int ldr = __ffs(mm) - 1;
-      if ((int)lane == ldr) qb = atomicAdd(&a.work->nbig, (uint32_t)__popc(mm));
-      qb = __shfl_sync(FULL_MASK, qb, ldr);
-      if (many) {
-        const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
-        if (q < a.big_cap) a.big[q] = r;
-        else atomicMax(&a.work->big_need, q + 1);
       }
     }
+    const int wt = __reduce_add_sync(FULL_MASK, ntpf);
+    if (lane == 0 && wt) atomicAdd(&a.work->tpf, (unsigned long long)wt);
   }
 }
 
@@ -825,7 +978,10 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const Fram
     a.result->rec_need = w->rec_need;
     a.result->big_need = w->big_need;
     a.result->error = w->error;
+    a.result->nclip = w->nclip;
+    a.result->clip_need = w->clip_need;
     w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
+    w->nclip = 0; w->clip_need = 0;
   }
   __syncthreads();
 
@@ -1010,9 +1166,17 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
   int n = 0;
   if (events) cudaEventRecord((cudaEvent_t)events[0], s);
   if (a.total_blocks > 0) {
+    if (a.light_blocks > 0) {
+      k_light<<<a.light_blocks, 256, 0, s>>>(a);
+      ++n;
+    }
     k_project<<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
+    if (a.flags & 0x01u) {
+      k_clip<<<kClipBlocks, 128, 0, s>>>(a);
+      ++n;
+    }
     k_bin_big<<<big_blocks, 256, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[2], s);
