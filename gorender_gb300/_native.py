@@ -33,7 +33,7 @@ EXPORTS = [
     "gr_renderer_set_fov", "gr_renderer_set_light", "gr_renderer_draw", "gr_renderer_read",
     "gr_renderer_tpf", "gr_context_event_record", "gr_context_event_elapsed", "gr_context_flush_l2",
     "gr_context_last_launches", "gr_context_last_transfer_bytes", "gr_draw_profiled", "gr_host_alloc",
-    "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning",
+    "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning", "gr_draw_noalloc",
 ]
 
 
@@ -68,6 +68,17 @@ class Object(C.Structure):
 
 class Camera(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("up", C.c_float * 3)]
+
+
+class NoallocObject(C.Structure):
+    """gr_noalloc_object: a mesh given by device pointers plus its matrices."""
+    _fields_ = [("mesh", MeshDesc), ("bbox", C.c_float * 32), ("mvp", C.c_float * 16),
+                ("world", C.c_float * 16)]
+
+
+class NoallocTexture(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("scale", C.c_float),
+                ("color", C.c_uint8 * 4), ("rgba", C.c_void_p)]
 
 
 _lib = None
@@ -117,6 +128,8 @@ def lib() -> C.CDLL:
             "gr_host_free": [vp],
             "gr_context_set_tuning": [vp, i32, i32],
             "gr_context_get_tuning": [vp, C.POINTER(i32), C.POINTER(i32)],
+            "gr_draw_noalloc": [i32, C.POINTER(NoallocObject), i32, C.POINTER(NoallocTexture), i32,
+                                C.POINTER(FrameParams), vp, vp, vp, C.POINTER(C.c_int64)],
         }
         for name, args in sig.items():
             f = getattr(L, name)

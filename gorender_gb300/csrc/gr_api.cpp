@@ -456,6 +456,18 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
 
 }  // namespace
 
+namespace gr {
+int32_t set_error(int32_t code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+}  // namespace gr
+
 extern "C" {
 
 const char* gr_last_error(void) { return g_err.c_str(); }

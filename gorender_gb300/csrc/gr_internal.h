@@ -146,4 +146,7 @@ struct FrameArgs {
 // after k_bin_big and after k_raster.
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events);
 
+// Records a message for gr_last_error() on this thread and returns code (gr_api.cpp).
+int32_t set_error(int32_t code, const char* fmt, ...);
+
 }  // namespace gr

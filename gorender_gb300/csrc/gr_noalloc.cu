@@ -1,0 +1,264 @@
+// gr_noalloc.cu -- gr_draw_noalloc: one frame with no device allocation.
+//
+// Who needs this: callers that must not call cudaMalloc/cudaFree, such as a
+// render thread inside an engine or framework whose allocator owns all device
+// memory, or a frame loop with a fixed memory budget where an allocation (and
+// the device synchronisation cudaFree implies) would stall the frame.  They
+// pass device pointers for every input and output; this entry point renders
+// the frame with the same kernels as gr_draw, but all of the frame's working
+// memory (triangle records, tile bins, queues, split-tile keys, counters,
+// the item and texture tables) is carved from one file-scope device array of
+// kScratchBytes (8 MiB).  Every GPU that loads the library holds that array
+// until the process exits.
+//
+// Limits (larger frames are rejected with GR_ERR_UNSUPPORTED): at most
+// kMaxFaces faces per frame, kMaxObjects objects, kMaxTextures textures,
+// kMaxNormals vertex normals across Gouraud-lit objects, and a framebuffer of
+// at most kMaxSide x kMaxSide pixels.  Bins and record buffers cannot grow
+// here: a frame that would overflow them returns GR_ERR_BIN_OVERFLOW.
+//
+// The array is shared by every call in the process: each call clears the
+// parts that must start at zero, and calls whose work overlaps on the GPU
+// (different streams, or different host threads on one device) race on it.
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress while that device is current; make that first call
+// before any stream capture.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/gorender_cuda.h"
+#include "gr_host_math.h"
+#include "gr_internal.h"
+
+namespace gr {
+namespace {
+
+constexpr int kMaxFaces = 4096;
+constexpr int kMaxObjects = 16;
+constexpr int kMaxTextures = 16;
+constexpr int kMaxNormals = 16384;
+constexpr int kMaxSide = 512;
+constexpr int kTiles = (kMaxSide / 32) * (kMaxSide / 32);
+constexpr uint32_t kRecCap = 3u * kMaxFaces;
+constexpr uint32_t kKeyCap = (uint32_t)kKeysPerFace * kMaxFaces + kKeysPerFace;
+constexpr uint32_t kBinCap = 1024;
+constexpr uint32_t kQueueCap = kMaxFaces + 1024;
+constexpr size_t kScratchBytes = 8u << 20;
+
+__device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Byte offsets of the sub-buffers inside g_scratch.
+struct Layout {
+  size_t items, texs, rast, shade, wide, tcol, keys, bins, bin_count, big, clip, vlight, gkey, tile_done, work,
+      result, end;
+};
+
+constexpr Layout make_layout() {
+  Layout l{};
+  size_t o = 0;
+  l.items = o; o += up256(sizeof(DevItem) * kMaxObjects);
+  l.texs = o; o += up256(sizeof(DevTex) * kMaxTextures);
+  l.rast = o; o += up256(sizeof(TriRaster) * kRecCap);
+  l.shade = o; o += up256(sizeof(TriShade) * kRecCap);
+  l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
+  l.tcol = o; o += up256(sizeof(TriColor) * kRecCap);
+  l.keys = o; o += up256(sizeof(uint32_t) * kKeyCap);
+  l.bins = o; o += up256(sizeof(uint32_t) * kTiles * kBinCap);
+  l.bin_count = o; o += up256(sizeof(uint32_t) * kTiles);
+  l.big = o; o += up256(sizeof(uint32_t) * kQueueCap);
+  l.clip = o; o += up256(sizeof(uint2) * kQueueCap);
+  l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
+  l.gkey = o; o += up256(sizeof(unsigned long long) * kTiles * 1024);
+  l.tile_done = o; o += up256(sizeof(uint32_t) * kTiles);
+  l.work = o; o += up256(sizeof(DevWork));
+  l.result = o; o += up256(sizeof(DevResult));
+  l.end = o;
+  return l;
+}
+constexpr Layout kLayout = make_layout();
+static_assert(kLayout.end <= kScratchBytes, "scratch layout exceeds the static array");
+
+std::mutex g_mu;
+unsigned char* g_ptr[64] = {};  // device address of g_scratch per device
+
+}  // namespace
+}  // namespace gr
+
+using namespace gr;
+
+extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* objects, int32_t num_objects,
+                                   const gr_noalloc_texture* textures, int32_t num_textures,
+                                   const gr_frame_params* p, uint8_t* rgba_dev, float* z_dev, void* stream,
+                                   int64_t* tpf_out) {
+  if (!p || !rgba_dev || !z_dev || num_objects < 0 || (num_objects > 0 && !objects) || num_textures < 0 ||
+      (num_textures > 0 && !textures))
+    return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: missing argument");
+  if (device < 0 || device >= 64) return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: bad device %d", device);
+  if (p->width <= 0 || p->height <= 0 || p->width > kMaxSide || p->height > kMaxSide)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: framebuffer %dx%d exceeds the %dx%d limit", p->width,
+                     p->height, kMaxSide, kMaxSide);
+  if (num_objects > kMaxObjects)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %d objects exceed the limit of %d", num_objects, kMaxObjects);
+  if (num_textures > kMaxTextures)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %d textures exceed the limit of %d", num_textures,
+                     kMaxTextures);
+  if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
+    return set_error(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
+  const bool gouraud_frame = (p->flags & GR_LIGHTING) && !(p->flags & GR_FLAT_SHADING);
+  long faces = 0, normals = 0;
+  for (int i = 0; i < num_objects; ++i) {
+    const gr_mesh_desc& m = objects[i].mesh;
+    if (m.num_faces < 0 || m.num_vertices <= 0 || !m.positions || (m.num_faces > 0 && (!m.vertex_indices || !m.face_normals)))
+      return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: object %d needs positions, vertex indices and face normals", i);
+    if (gouraud_frame && m.num_normals > 0 && (!m.vertex_normals || !m.normal_indices))
+      return set_error(GR_ERR_BAD_INDEX, "gr_draw_noalloc: object %d has vertex normals without normal indices", i);
+    faces += m.num_faces;
+    if (gouraud_frame) normals += m.num_normals;
+  }
+  if (faces > kMaxFaces)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld faces exceed the limit of %d", faces, kMaxFaces);
+  if (normals > kMaxNormals)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld vertex normals exceed the limit of %d", normals,
+                     kMaxNormals);
+
+  std::lock_guard<std::mutex> lk(g_mu);
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return set_error(GR_ERR_NO_DEVICE, "gr_draw_noalloc: cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+  if (!g_ptr[device]) {
+    // once per device, with that device current
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_scratch);
+    if (e != cudaSuccess) {
+      if (prev >= 0) cudaSetDevice(prev);
+      return set_error(GR_ERR_CUDA, "gr_draw_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    }
+    g_ptr[device] = (unsigned char*)ptr;
+  }
+  unsigned char* base = g_ptr[device];
+  cudaStream_t s = (cudaStream_t)stream;
+
+  // host staging of the item and texture tables (plain stack arrays)
+  DevItem items[kMaxObjects];
+  DevTex texs[kMaxTextures];
+  std::memset(items, 0, sizeof(items));
+  std::memset(texs, 0, sizeof(texs));
+  int live = 0, blocks = 0, light_blocks = 0, light_total = 0;
+  uint32_t face_base = 0;
+  for (int i = 0; i < num_objects; ++i) {
+    const gr_mesh_desc& m = objects[i].mesh;
+    const uint32_t fb = face_base;
+    face_base += (uint32_t)m.num_faces;
+    if (m.num_faces == 0) continue;
+    DevItem& d = items[live++];
+    std::memcpy(d.mvp, objects[i].mvp, sizeof(d.mvp));
+    std::memcpy(d.world, objects[i].world, sizeof(d.world));
+    std::memcpy(d.bbox, objects[i].bbox, sizeof(d.bbox));
+    d.pos = m.positions; d.vnrm = m.vertex_normals; d.fnrm = m.face_normals; d.vidx = m.vertex_indices;
+    d.nidx = m.normal_indices; d.uv = m.uvs; d.tex = m.face_textures; d.vcol = m.vertex_colors;
+    d.nv = m.num_vertices; d.nn = m.vertex_normals ? m.num_normals : 0; d.nf = m.num_faces;
+    d.face_base = fb;
+    d.block_base = blocks;
+    blocks += (m.num_faces + kProjectThreads - 1) / kProjectThreads;
+    d.light_base = light_total;
+    d.light_block_base = light_blocks;
+    if (gouraud_frame && d.nn > 0) {
+      light_total += d.nn;
+      light_blocks += (d.nn + 255) / 256;
+    }
+  }
+  for (int i = 0; i < num_textures; ++i) {
+    const gr_noalloc_texture& t = textures[i];
+    DevTex& d = texs[i];
+    d.kind = t.kind;
+    d.scale = t.scale;
+    d.color = (uint32_t)t.color[0] | ((uint32_t)t.color[1] << 8) | ((uint32_t)t.color[2] << 16) |
+              ((uint32_t)t.color[3] << 24);
+    if (t.kind != GR_TEXTURE_SOLID) {
+      const bool pow2 = t.width > 0 && t.height > 0 && (t.width & (t.width - 1)) == 0 && (t.height & (t.height - 1)) == 0;
+      if (!t.rgba || t.width <= 0 || t.height <= 0 || (t.kind == GR_TEXTURE_IMAGE_FAST && !pow2) ||
+          (t.kind != GR_TEXTURE_IMAGE && t.kind != GR_TEXTURE_IMAGE_FAST)) {
+        if (prev >= 0) cudaSetDevice(prev);
+        return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: bad texture %d", i);
+      }
+      d.width = t.width;
+      d.height = t.height;
+      d.widthF = (float)t.width;
+      d.heightF = (float)t.height;
+      d.px = (const uint32_t*)t.rgba;
+    }
+  }
+
+  FrameArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.W = p->width;
+  a.H = p->height;
+  a.flags = p->flags;
+  a.tile_shift = 5;
+  a.tiles_x = (p->width + 31) / 32;
+  a.tiles_y = (p->height + 31) / 32;
+  a.num_items = live;
+  a.total_blocks = blocks;
+  a.bin_cap = kBinCap;
+  a.rec_cap = kRecCap;
+  a.big_cap = kQueueCap;
+  a.key_cap = kKeyCap;
+  a.clip_cap = kQueueCap;
+  a.slice_entries = kDefaultSliceEntries;
+  a.light_blocks = light_blocks;
+  for (int k = 0; k < 8; ++k) a.S[k] = p->screen[k];
+  for (int k = 0; k < 3; ++k) a.L[k] = p->light[k];
+  a.items = (const DevItem*)(base + kLayout.items);
+  a.texs = (const DevTex*)(base + kLayout.texs);
+  a.num_tex = num_textures;
+  a.rast = (TriRaster*)(base + kLayout.rast);
+  a.shade = (TriShade*)(base + kLayout.shade);
+  a.wide = (TriWide*)(base + kLayout.wide);
+  a.tcol = (TriColor*)(base + kLayout.tcol);
+  a.rec_of_key = (uint32_t*)(base + kLayout.keys);
+  a.bins = (uint32_t*)(base + kLayout.bins);
+  a.bin_count = (uint32_t*)(base + kLayout.bin_count);
+  a.big = (uint32_t*)(base + kLayout.big);
+  a.clip = (uint2*)(base + kLayout.clip);
+  a.vlight = (float*)(base + kLayout.vlight);
+  a.gkey = (unsigned long long*)(base + kLayout.gkey);
+  a.tile_done = (uint32_t*)(base + kLayout.tile_done);
+  a.work = (DevWork*)(base + kLayout.work);
+  a.result = (DevResult*)(base + kLayout.result);
+  a.out_rgba = (uint32_t*)rgba_dev;
+  a.out_z = z_dev;
+  a.vec_ok = (p->width % 4 == 0) && ((uintptr_t)rgba_dev % 16 == 0) && ((uintptr_t)z_dev % 16 == 0);
+
+  // The array keeps the previous call's contents: zero what the kernels
+  // expect to find zeroed (counters, bin counts, split-tile keys).
+  const int tiles = a.tiles_x * a.tiles_y;
+  e = cudaMemsetAsync(base + kLayout.bin_count, 0, sizeof(uint32_t) * tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.gkey, 0, sizeof(unsigned long long) * tiles * 1024, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.tile_done, 0, sizeof(uint32_t) * tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.work, 0, sizeof(DevWork), s);
+  if (e == cudaSuccess && live) e = cudaMemcpyAsync(base + kLayout.items, items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && num_textures)
+    e = cudaMemcpyAsync(base + kLayout.texs, texs, sizeof(DevTex) * num_textures, cudaMemcpyHostToDevice, s);
+  int launches = 0;
+  if (e == cudaSuccess) e = (cudaError_t)launch_frame(a, 2 * 152, s, &launches, nullptr);
+  DevResult r;
+  std::memset(&r, 0, sizeof(r));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&r, base + kLayout.result, sizeof(r), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (prev >= 0) cudaSetDevice(prev);
+  if (e != cudaSuccess) return set_error(GR_ERR_CUDA, "gr_draw_noalloc: %s", cudaGetErrorString(e));
+  if (r.error & 1u) return set_error(GR_ERR_CLIP_OVERFLOW, "a clipped polygon exceeded 9 vertices");
+  if (r.bin_need > kBinCap || r.rec_need > kRecCap || r.big_need > kQueueCap || r.clip_need > kQueueCap)
+    return set_error(GR_ERR_BIN_OVERFLOW, "gr_draw_noalloc: the frame needs more working memory than the %zu-byte "
+                     "static array provides (bins %u/%u, records %u/%u)", kScratchBytes, r.bin_need, kBinCap,
+                     r.rec_need, kRecCap);
+  if (tpf_out) *tpf_out = (int64_t)r.tpf;
+  return GR_OK;
+}

@@ -206,6 +206,51 @@ int32_t gr_draw_profiled(gr_context* ctx, const gr_draw_item* items, int32_t num
 int32_t gr_host_alloc(int64_t bytes, void** out);
 int32_t gr_host_free(void* p);
 
+/* ---- draw without allocating: no counterpart in the reference ----
+ * For callers that must not allocate device memory themselves or let a
+ * library do it: an engine or framework that owns every device allocation,
+ * or a frame loop with a fixed memory budget in which a cudaMalloc/cudaFree
+ * (and the device synchronisation cudaFree implies) would stall the frame.
+ * gr_draw_noalloc renders one frame like gr_draw, with every input and output
+ * in caller-owned device memory, and takes all of its working memory from one
+ * static device array of 8 MiB inside the library (held by every GPU that
+ * loads the library until the process exits).  It allocates nothing.
+ *
+ * Limits, checked up front (GR_ERR_UNSUPPORTED): <= 4096 faces per frame,
+ * <= 16 objects, <= 16 textures, <= 16384 vertex normals across Gouraud-lit
+ * objects, framebuffer <= 512 x 512.  A frame that overflows the fixed bins
+ * or record buffers returns GR_ERR_BIN_OVERFLOW (nothing can grow here).
+ * Device-side inputs are not validated: vertex/normal indices must be in
+ * range and face texture handles must index `textures`.
+ *
+ * Concurrency: all calls share the static array (each call clears what must
+ * start at zero); calls whose GPU work overlaps (other streams, other host
+ * threads on the same device) race on it.  The call is synchronous: it waits
+ * for `stream` (a cudaStream_t; NULL = default stream) before returning.  The
+ * first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make it before any
+ * stream capture. */
+typedef struct {
+  gr_mesh_desc mesh;  /* DEVICE pointers; face_normals is required (NewMesh normals);
+                         face_textures index the `textures` array, -1 = nil */
+  float bbox[32];     /* Mesh.BoundingBox, host memory (8 corners x 4) */
+  float mvp[16];      /* as gr_draw_item */
+  float world[16];
+} gr_noalloc_object;
+
+typedef struct {
+  int32_t kind;           /* GR_TEXTURE_* */
+  int32_t width, height;
+  float scale;
+  uint8_t color[4];       /* solid colour */
+  const uint8_t* rgba;    /* DEVICE pointer, width*height*4 bytes (image kinds) */
+} gr_noalloc_texture;
+
+int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* objects, int32_t num_objects,
+                        const gr_noalloc_texture* textures, int32_t num_textures,
+                        const gr_frame_params* params, uint8_t* rgba_dev, float* z_dev, void* stream,
+                        int64_t* tpf_out);
+
 #ifdef __cplusplus
 }
 #endif
