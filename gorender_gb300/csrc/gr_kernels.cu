@@ -1028,17 +1028,60 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const Fram
         tri[lane] = t;
         trec[lane] = r;
       }
+      // Flattened coverage walk: the chunk's (triangle, footprint pixel)
+      // pairs are numbered consecutively (a warp scan of the footprint
+      // areas) and each iteration tests 32 of them, so the warp runs
+      // ceil(total / 32) iterations rather than the largest footprint.
       const int my = by_lane ? area : 0;
-      const int iters = __reduce_max_sync(FULL_MASK, my);
-      int x = lx0, y = ly0;
-      for (int it = 0; it < iters; ++it) {
-        const bool c = it < my && t.a01 * x + t.b01 * y + t.c01 < 0 && t.a12 * x + t.b12 * y + t.c12 < 0 &&
-                       t.a20 * x + t.b20 * y + t.c20 < 0;
-        q.push(c, lane, x - tx0, y - ty0, skey, a, tx0, ty0);
-        if (++x > lx1) {
-          x = lx0;
-          ++y;
+      int incl = my;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, incl, o);
+        if ((int)lane >= o) incl += y;
+      }
+      const int excl = incl - my;
+      const int total = __shfl_sync(FULL_MASK, incl, 31);
+      const int bw = lx1 - lx0 + 1;                       // footprint width, <= TS
+      const int magic = by_lane ? (65536 + bw - 1) / bw : 0;  // exact o / bw for o < 2048
+      __syncwarp();
+      const int widest = __reduce_max_sync(FULL_MASK, my);
+      if (((total + 31) >> 5) * 9 >= widest * 5) {
+        // footprints of similar size: one lane per triangle is cheaper
+        int x = lx0, y = ly0;
+        for (int it = 0; it < widest; ++it) {
+          const bool c = it < my && t.a01 * x + t.b01 * y + t.c01 < 0 && t.a12 * x + t.b12 * y + t.c12 < 0 &&
+                         t.a20 * x + t.b20 * y + t.c20 < 0;
+          q.push(c, lane, x - tx0, y - ty0, skey, a, tx0, ty0);
+          if (++x > lx1) {
+            x = lx0;
+            ++y;
+          }
         }
+      } else
+      for (int g0 = 0; g0 < total; g0 += 32) {
+        const int g = g0 + (int)lane;
+        // owner: the last lane whose range starts at or before g (zero-area
+        // lanes share the next lane's start and are never chosen)
+        int own = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int cand = own + step;
+          const int ce = __shfl_sync(FULL_MASK, excl, cand & 31);
+          if (cand < 32 && ce <= g) own = cand;
+        }
+        const int o = g - __shfl_sync(FULL_MASK, excl, own);
+        const int ow = __shfl_sync(FULL_MASK, bw, own);
+        const int om = __shfl_sync(FULL_MASK, magic, own);
+        const int ox = __shfl_sync(FULL_MASK, lx0, own), oy = __shfl_sync(FULL_MASK, ly0, own);
+        const int dy = (o * om) >> 16;
+        const int x = ox + (o - dy * ow), y = oy + dy;
+        bool c = false;
+        if (g < total) {
+          const TriRaster& tt = tri[own];
+          c = tt.a01 * x + tt.b01 * y + tt.c01 < 0 && tt.a12 * x + tt.b12 * y + tt.c12 < 0 &&
+              tt.a20 * x + tt.b20 * y + tt.c20 < 0;
+        }
+        q.push(c, (uint32_t)own, x - tx0, y - ty0, skey, a, tx0, ty0);
       }
       q.flush(skey, a, tx0, ty0);  // lane slots are rewritten by the next chunk
     }
