@@ -34,6 +34,8 @@ EXPORTS = [
     "gr_renderer_tpf", "gr_context_event_record", "gr_context_event_elapsed", "gr_context_flush_l2",
     "gr_context_last_launches", "gr_context_last_transfer_bytes", "gr_draw_profiled", "gr_host_alloc",
     "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning", "gr_draw_noalloc",
+    "gr_draw_views", "gr_context_view_tpf", "gr_batch_create", "gr_batch_run", "gr_batch_sync",
+    "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_autotune",
 ]
 
 
@@ -68,6 +70,11 @@ class Object(C.Structure):
 
 class Camera(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("up", C.c_float * 3)]
+
+
+class View(C.Structure):
+    """gr_view: one view of a batch."""
+    _fields_ = [("params", FrameParams), ("rgba_dev", C.c_void_p), ("z_dev", C.c_void_p)]
 
 
 class NoallocObject(C.Structure):
@@ -130,6 +137,15 @@ def lib() -> C.CDLL:
             "gr_context_get_tuning": [vp, C.POINTER(i32), C.POINTER(i32)],
             "gr_draw_noalloc": [i32, C.POINTER(NoallocObject), i32, C.POINTER(NoallocTexture), i32,
                                 C.POINTER(FrameParams), vp, vp, vp, C.POINTER(C.c_int64)],
+            "gr_draw_views": [vp, C.POINTER(View), i32, C.POINTER(DrawItem), i32],
+            "gr_context_view_tpf": [vp, C.POINTER(C.c_int64), i32],
+            "gr_batch_create": [vp, C.POINTER(View), i32, C.POINTER(DrawItem), i32, i32, C.POINTER(vp)],
+            "gr_batch_run": [vp],
+            "gr_batch_sync": [vp],
+            "gr_batch_tuning": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), fp],
+            "gr_batch_destroy": [vp],
+            "gr_context_set_raster": [vp, i32, i32],
+            "gr_context_autotune": [vp, C.POINTER(DrawItem), i32, C.POINTER(FrameParams)],
         }
         for name, args in sig.items():
             f = getattr(L, name)

@@ -87,7 +87,7 @@ struct gr_context {
   uint32_t* bin_count = nullptr;
   uint32_t bin_cap = 0;
   uint32_t tiles_cap = 0;
-  uint32_t* big = nullptr;
+  uint2* big = nullptr;             // multi-tile queue: (record, view)
   uint32_t big_cap = 0;
   unsigned long long* gkey = nullptr;  // merged keys of tiles split over several CTAs
   uint32_t* tile_done = nullptr;
@@ -96,6 +96,17 @@ struct gr_context {
   uint32_t clip_cap = 0;
   float* vlight = nullptr;          // per-normal Gouraud intensities
   uint64_t vlight_cap = 0;
+  DevView* d_views = nullptr;       // view table (device) and its pinned staging
+  DevView* h_views = nullptr;
+  unsigned long long* view_tpf = nullptr;
+  unsigned long long* view_tpf_out = nullptr;
+  unsigned long long* h_view_tpf = nullptr;
+  int views_cap = 0;
+  uint2* plan = nullptr;            // raster work queue
+  uint32_t plan_cap = 0;
+  int raster_waves = 1;             // persistent raster CTAs = SMs x resident CTAs x waves
+  int last_views = 0;               // views of the last batched draw
+  float tuned_ms = 0.0f;            // best batch time seen by the autotuner
   uint32_t slice_entries = kDefaultSliceEntries;
   DevWork* work = nullptr;
   DevResult* d_result = nullptr;
@@ -285,32 +296,106 @@ struct Prepared {
   int nitems;
 };
 
-// Validates the items, stages DevItems and fills the kernel arguments.
-int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p, Prepared& out) {
-  if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "params is NULL");
+// One view of a draw: its parameters and device outputs.
+struct ViewIn {
+  const gr_frame_params* p;
+  uint32_t* rgba;
+  float* z;
+};
+
+int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
+  if (nviews > c->views_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out);
+    if (c->h_views) cudaFreeHost(c->h_views);
+    if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
+    c->h_views = nullptr;
+    c->h_view_tpf = nullptr;
+    c->views_cap = 0;
+    const int cap = std::max(nviews, 2 * c->views_cap);
+    int32_t st;
+    if ((st = dev_alloc(&c->d_views, cap)) || (st = dev_alloc(&c->view_tpf, cap)) ||
+        (st = dev_alloc(&c->view_tpf_out, cap)))
+      return st;
+    CK(cudaMemsetAsync(c->view_tpf, 0, sizeof(unsigned long long) * cap, c->stream));
+    CK(cudaMallocHost((void**)&c->h_views, sizeof(DevView) * cap));
+    CK(cudaMallocHost((void**)&c->h_view_tpf, sizeof(unsigned long long) * cap));
+    c->views_cap = cap;
+  }
+  const uint64_t want_plan = (uint64_t)tiles * kRasterMaxSlices;
+  if (want_plan > c->plan_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->plan);
+    c->plan_cap = 0;
+    int32_t st = dev_alloc(&c->plan, want_plan);
+    if (st) return st;
+    c->plan_cap = (uint32_t)want_plan;
+  }
+  return GR_OK;
+}
+
+// Validates views and items, stages the view and item tables and fills the
+// kernel arguments.  items[i].reserved is the item's view when batched.
+int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_item* items, int32_t n, bool batched,
+                Prepared& out, DevView* own_views = nullptr, DevItem* own_items = nullptr) {
+  if (nviews <= 0 || !views) return fail(GR_ERR_INVALID_ARGUMENT, "no views");
   if (n < 0 || (n > 0 && !items)) return fail(GR_ERR_INVALID_ARGUMENT, "bad item list");
-  if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size %dx%d", p->width, p->height);
-  if (p->width > kMaxDim || p->height > kMaxDim)
-    return fail(GR_ERR_UNSUPPORTED, "framebuffer %dx%d exceeds %d", p->width, p->height, kMaxDim);
-  if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
-    return fail(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
+  const int ts = 1 << c->tile_shift;
+  uint32_t total_tiles = 0, flags_any = 0;
+  for (int v = 0; v < nviews; ++v) {
+    const gr_frame_params* p = views[v].p;
+    if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "view %d: params is NULL", v);
+    if (p->width <= 0 || p->height <= 0)
+      return fail(GR_ERR_INVALID_ARGUMENT, "view %d: bad framebuffer size %dx%d", v, p->width, p->height);
+    if (p->width > kMaxDim || p->height > kMaxDim)
+      return fail(GR_ERR_UNSUPPORTED, "view %d: framebuffer %dx%d exceeds %d", v, p->width, p->height, kMaxDim);
+    if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
+      return fail(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
+    if (!views[v].rgba || !views[v].z) return fail(GR_ERR_INVALID_ARGUMENT, "view %d: missing outputs", v);
+    const uint64_t t = (uint64_t)((p->width + ts - 1) / ts) * (uint64_t)((p->height + ts - 1) / ts);
+    if (total_tiles + t >= (1ull << 31)) return fail(GR_ERR_UNSUPPORTED, "too many raster tiles");
+    total_tiles += (uint32_t)t;
+    flags_any |= p->flags;
+  }
   int32_t st = ensure_items(c, std::max(n, 1));
   if (st) return st;
   if ((st = upload_textures(c))) return st;
-  const bool gouraud = (p->flags & GR_LIGHTING) && !(p->flags & GR_FLAT_SHADING);
+  if ((st = ensure_views(c, nviews, total_tiles))) return st;
+  uint32_t tile_base = 0;
+  for (int v = 0; v < nviews; ++v) {
+    const gr_frame_params* p = views[v].p;
+    DevView& d = c->h_views[v];
+    std::memset(&d, 0, sizeof(d));
+    d.W = p->width;
+    d.H = p->height;
+    d.flags = p->flags;
+    d.tiles_x = (p->width + ts - 1) / ts;
+    d.tiles_y = (p->height + ts - 1) / ts;
+    d.tile_base = tile_base;
+    tile_base += (uint32_t)(d.tiles_x * d.tiles_y);
+    for (int k = 0; k < 8; ++k) d.S[k] = p->screen[k];
+    for (int k = 0; k < 3; ++k) d.L[k] = p->light[k];
+    d.out_rgba = views[v].rgba;
+    d.out_z = views[v].z;
+    d.vec_ok = (p->width % 4 == 0) && ((uintptr_t)d.out_rgba % 16 == 0) && ((uintptr_t)d.out_z % 16 == 0);
+  }
   uint64_t faces = 0;
   int blocks = 0;
   int light_blocks = 0;
   uint64_t light_total = 0;
   int live = 0;
   for (int i = 0; i < n; ++i) {
-    int m = items[i].mesh;
+    const int m = items[i].mesh;
     if (m < 0 || m >= (int)c->meshes.size() || !c->meshes[m].alive)
       return fail(GR_ERR_INVALID_ARGUMENT, "item %d: unknown mesh %d", i, m);
+    const int view = batched ? items[i].reserved : 0;
+    if (view < 0 || view >= nviews) return fail(GR_ERR_INVALID_ARGUMENT, "item %d: view %d of %d", i, view, nviews);
+    const uint32_t fl = views[view].p->flags;
+    const bool gouraud = (fl & GR_LIGHTING) && !(fl & GR_FLAT_SHADING);
     const MeshRec& mr = c->meshes[m];
     if (gouraud && mr.nn > 0 && !mr.nidx_ok)
       return fail(GR_ERR_BAD_INDEX, "item %d: mesh %d has missing or out-of-range normal indices", i, m);
-    uint64_t fb = faces;
+    const uint64_t fb = faces;
     faces += (uint64_t)mr.nf;
     if (mr.nf == 0) continue;  // an empty mesh draws nothing
     DevItem& d = c->h_items[live++];
@@ -322,6 +407,7 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
     d.nv = mr.nv; d.nn = mr.nn; d.nf = mr.nf;
     d.face_base = (uint32_t)fb;
     d.block_base = blocks;
+    d.view = view;
     blocks += (mr.nf + kProjectThreads - 1) / kProjectThreads;
     // every item gets a k_light block range (empty for non-Gouraud items) so the
     // kernel's block -> item search sees non-decreasing bases
@@ -333,10 +419,7 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
     }
   }
   if (faces >= (1ull << 28)) return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces in one frame");
-  const int ts = 1 << c->tile_shift;
-  const int tiles_x = (p->width + ts - 1) / ts;
-  const int tiles_y = (p->height + ts - 1) / ts;
-  if ((st = ensure_frame_buffers(c, faces, (uint32_t)(tiles_x * tiles_y)))) return st;
+  if ((st = ensure_frame_buffers(c, faces, total_tiles))) return st;
   if (light_total > c->vlight_cap) {
     CK(cudaStreamSynchronize(c->stream));
     dev_free(c->vlight);
@@ -344,17 +427,20 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
     if ((st = dev_alloc(&c->vlight, light_total))) return st;
     c->vlight_cap = light_total;
   }
-  if (live) CK(cudaMemcpyAsync(c->d_items, c->h_items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
-  c->h2d_bytes = (int64_t)sizeof(DevItem) * live;
+  // a graph batch keeps its own tables, so other draws cannot overwrite them
+  DevView* dviews = own_views ? own_views : c->d_views;
+  DevItem* ditems = own_items ? own_items : c->d_items;
+  CK(cudaMemcpyAsync(dviews, c->h_views, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
+  if (live) CK(cudaMemcpyAsync(ditems, c->h_items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+  c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
   c->d2h_bytes = 0;
 
   FrameArgs& a = out.a;
   std::memset(&a, 0, sizeof(a));
-  a.W = p->width;
-  a.H = p->height;
-  a.flags = p->flags;
-  a.tiles_x = tiles_x;
-  a.tiles_y = tiles_y;
+  a.views = dviews;
+  a.num_views = nviews;
+  a.total_tiles = total_tiles;
+  a.flags_any = flags_any;
   a.tile_shift = c->tile_shift;
   a.num_items = live;
   a.total_blocks = blocks;
@@ -362,9 +448,7 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   a.rec_cap = c->rec_cap;
   a.big_cap = c->big_cap;
   a.key_cap = c->key_cap;
-  for (int k = 0; k < 8; ++k) a.S[k] = p->screen[k];
-  for (int k = 0; k < 3; ++k) a.L[k] = p->light[k];
-  a.items = c->d_items;
+  a.items = ditems;
   a.texs = c->d_texs;
   a.num_tex = (int)c->texs.size();
   a.rast = c->rast;
@@ -384,15 +468,14 @@ int32_t prepare(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
   a.light_blocks = light_blocks;
   a.work = c->work;
   a.result = c->d_result;
+  a.view_tpf = c->view_tpf;
+  a.view_tpf_out = c->view_tpf_out;
+  a.plan = c->plan;
+  a.plan_cap = c->plan_cap;
+  a.raster_ctas = raster_grid(c->tile_shift, c->raster_waves);
   out.faces = faces;
   out.nitems = live;
   return GR_OK;
-}
-
-void set_outputs(FrameArgs& a, uint32_t* rgba, float* z) {
-  a.out_rgba = rgba;
-  a.out_z = z;
-  a.vec_ok = (a.W % 4 == 0) && ((uintptr_t)rgba % 16 == 0) && ((uintptr_t)z % 16 == 0);
 }
 
 int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr) {
@@ -400,6 +483,24 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
   int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
   return GR_OK;
+}
+
+// Identity of every context buffer a captured graph refers to: a graph whose
+// signature no longer matches must be captured again before it runs.
+uint64_t buffers_signature(const gr_context* c) {
+  const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->wide, (uintptr_t)c->tcol,
+                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->gkey,
+                          (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->big, (uintptr_t)c->vlight,
+                          (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
+                          (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, c->rec_cap, c->key_cap, c->bin_cap,
+                          c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_entries,
+                          (uintptr_t)c->raster_waves, c->texs.size()};
+  uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
+  for (uintptr_t v : ps) {
+    h ^= (uint64_t)v;
+    h *= 1099511628211ull;
+  }
+  return h;
 }
 
 // Reads the frame result; grows buffers that overflowed.  Returns 1 when the
@@ -417,20 +518,22 @@ int check_result(gr_context* c, const DevResult& r, int32_t* err) {
 
 int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p,
                   uint8_t* rgba_out, float* z_out, int64_t* tpf_out) {
+  if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "params is NULL");
   const size_t px = (size_t)p->width * (size_t)p->height;
   const bool rgba_dev = is_device_ptr(rgba_out), z_dev = is_device_ptr(z_out);
   int32_t st;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    Prepared pr;
-    if ((st = prepare(c, items, n, p, pr))) return st;
     uint32_t* rgba = rgba_dev ? (uint32_t*)rgba_out : nullptr;
     float* z = z_dev ? z_out : nullptr;
     if (!rgba || !z) {
+      if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
       if ((st = ensure_fb(c, px))) return st;
       if (!rgba) rgba = c->fb_rgba;
       if (!z) z = c->fb_z;
     }
-    set_outputs(pr.a, rgba, z);
+    ViewIn v{p, rgba, z};
+    Prepared pr;
+    if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
     if ((st = launch(c, pr.a))) return st;
     CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -515,6 +618,9 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
+  dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan);
+  if (c->h_views) cudaFreeHost(c->h_views);
+  if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
   dev_free(c->work); dev_free(c->d_result);
   if (c->h_result) cudaFreeHost(c->h_result);
   dev_free(c->fb_rgba); dev_free(c->fb_z);
@@ -654,24 +760,26 @@ int32_t gr_draw(gr_context* c, const gr_draw_item* items, int32_t n, const gr_fr
 
 int32_t gr_draw_async(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p,
                       uint8_t* rgba_dev, float* z_dev) {
-  if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  if (!c || !p) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   if ((rgba_dev && !is_device_ptr(rgba_dev)) || (z_dev && !is_device_ptr(z_dev)))
     return fail(GR_ERR_INVALID_ARGUMENT, "gr_draw_async needs device output pointers");
-  Prepared pr;
-  int32_t st = prepare(c, items, n, p, pr);
-  if (st) return st;
+  int32_t st;
   const size_t px = (size_t)p->width * (size_t)p->height;
-  if (!rgba_dev || !z_dev)
+  if (!rgba_dev || !z_dev) {
+    if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
     if ((st = ensure_fb(c, px))) return st;
-  set_outputs(pr.a, rgba_dev ? (uint32_t*)rgba_dev : c->fb_rgba, z_dev ? z_dev : c->fb_z);
+  }
+  ViewIn v{p, rgba_dev ? (uint32_t*)rgba_dev : c->fb_rgba, z_dev ? z_dev : c->fb_z};
+  Prepared pr;
+  if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
   return launch(c, pr.a);
 }
 
 int32_t gr_draw_profiled(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p,
                          uint8_t* rgba_dev, float* z_dev, float* kernel_ms3) {
-  if (!c || !kernel_ms3) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!c || !kernel_ms3 || !p) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   if ((rgba_dev && !is_device_ptr(rgba_dev)) || (z_dev && !is_device_ptr(z_dev)))
@@ -679,11 +787,13 @@ int32_t gr_draw_profiled(gr_context* c, const gr_draw_item* items, int32_t n, co
   const size_t px = (size_t)p->width * (size_t)p->height;
   int32_t st;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    Prepared pr;
-    if ((st = prepare(c, items, n, p, pr))) return st;
-    if (!rgba_dev || !z_dev)
+    if (!rgba_dev || !z_dev) {
+      if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
       if ((st = ensure_fb(c, px))) return st;
-    set_outputs(pr.a, rgba_dev ? (uint32_t*)rgba_dev : c->fb_rgba, z_dev ? z_dev : c->fb_z);
+    }
+    ViewIn v{p, rgba_dev ? (uint32_t*)rgba_dev : c->fb_rgba, z_dev ? z_dev : c->fb_z};
+    Prepared pr;
+    if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
     void* ev[4] = {c->events[60], c->events[61], c->events[62], c->events[63]};
     if ((st = launch(c, pr.a, ev))) return st;
     CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
@@ -696,6 +806,262 @@ int32_t gr_draw_profiled(gr_context* c, const gr_draw_item* items, int32_t n, co
     return GR_OK;
   }
   return fail(GR_ERR_OUT_OF_MEMORY, "frame buffers kept overflowing after resizing");
+}
+
+// ---- batched views ----
+
+static int32_t views_in(gr_context* c, const gr_view* views, int32_t nv, std::vector<ViewIn>& out) {
+  if (nv <= 0 || !views) return fail(GR_ERR_INVALID_ARGUMENT, "no views");
+  out.resize((size_t)nv);
+  for (int v = 0; v < nv; ++v) {
+    if (!views[v].rgba_dev || !views[v].z_dev || !is_device_ptr(views[v].rgba_dev) || !is_device_ptr(views[v].z_dev))
+      return fail(GR_ERR_INVALID_ARGUMENT, "view %d: outputs must be device pointers", v);
+    out[v] = ViewIn{&views[v].params, (uint32_t*)views[v].rgba_dev, views[v].z_dev};
+  }
+  (void)c;
+  return GR_OK;
+}
+
+int32_t gr_draw_views(gr_context* c, const gr_view* views, int32_t nviews, const gr_draw_item* items, int32_t n) {
+  if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  std::vector<ViewIn> vin;
+  int32_t st = views_in(c, views, nviews, vin);
+  if (st) return st;
+  Prepared pr;
+  if ((st = prepare(c, vin.data(), nviews, items, n, true, pr))) return st;
+  if ((st = launch(c, pr.a))) return st;
+  CK(cudaMemcpyAsync(c->h_view_tpf, c->view_tpf_out, sizeof(unsigned long long) * nviews, cudaMemcpyDeviceToHost,
+                     c->stream));
+  c->last_views = nviews;
+  return GR_OK;
+}
+
+int32_t gr_context_view_tpf(gr_context* c, int64_t* tpf, int32_t nviews) {
+  if (!c || !tpf || nviews < 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (nviews > c->last_views) return fail(GR_ERR_INVALID_ARGUMENT, "last batch had %d views", c->last_views);
+  for (int v = 0; v < nviews; ++v) tpf[v] = (int64_t)c->h_view_tpf[v];
+  return GR_OK;
+}
+
+}  // extern "C"
+
+struct gr_batch {
+  gr_context* ctx = nullptr;
+  std::vector<gr_view> views;
+  std::vector<ViewIn> vin;
+  std::vector<gr_draw_item> items;
+  DevView* d_views = nullptr;  // the batch's own view and item tables
+  DevItem* d_items = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t signature = 0;      // buffers_signature() at capture
+  int launches = 0;
+};
+
+namespace {
+
+void batch_drop_graph(gr_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+// Stages the batch's tables (outside any capture) and captures its frame
+// kernels plus the result copies as a CUDA graph.
+int32_t batch_capture(gr_batch* b) {
+  gr_context* c = b->ctx;
+  batch_drop_graph(b);
+  const int nv = (int)b->views.size();
+  for (int v = 0; v < nv; ++v) b->vin[v].p = &b->views[v].params;
+  if (!b->d_views) {
+    int32_t st = dev_alloc(&b->d_views, (size_t)nv);
+    if (!st) st = dev_alloc(&b->d_items, std::max<size_t>(1, b->items.size()));
+    if (st) return st;
+  }
+  Prepared pr;
+  int32_t st = prepare(c, b->vin.data(), nv, b->items.data(), (int)b->items.size(), true, pr, b->d_views, b->d_items);
+  if (st) return st;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int err = launch_frame(pr.a, 2 * 152, c->stream, &b->launches, nullptr);
+  cudaError_t e2 = cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e3 = cudaMemcpyAsync(c->h_view_tpf, c->view_tpf_out, sizeof(unsigned long long) * nv,
+                                   cudaMemcpyDeviceToHost, c->stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (err || e2 || e3 || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(GR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : (cudaError_t)(err ? err : (e2 ? e2 : e3))));
+  }
+  b->graph = g;
+  CK(cudaGraphInstantiate(&b->exec, g, 0));
+  b->signature = buffers_signature(c);
+  c->last_launches = b->launches;
+  c->last_views = nv;
+  return GR_OK;
+}
+
+// Runs the batch once without a graph, growing buffers until it fits; returns
+// the device time in ms of the final run.
+int32_t batch_run_plain(gr_batch* b, float* ms) {
+  gr_context* c = b->ctx;
+  const int nv = (int)b->views.size();
+  for (int attempt = 0; attempt < 5; ++attempt) {
+    Prepared pr;
+    int32_t st = prepare(c, b->vin.data(), nv, b->items.data(), (int)b->items.size(), true, pr);
+    if (st) return st;
+    CK(cudaEventRecord(c->events[58], c->stream));
+    if ((st = launch(c, pr.a))) return st;
+    CK(cudaEventRecord(c->events[59], c->stream));
+    CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int32_t err;
+    const int rerun = check_result(c, *c->h_result, &err);
+    if (err) return err;
+    if (rerun) continue;
+    if (ms) CK(cudaEventElapsedTime(ms, c->events[58], c->events[59]));
+    return GR_OK;
+  }
+  return fail(GR_ERR_OUT_OF_MEMORY, "batch buffers kept overflowing after resizing");
+}
+
+// Autotuner: raster tile size, slice length and persistent-grid waves, each
+// candidate timed on the batch itself (best of three runs); then the tile
+// bins are sized to the largest bin seen plus a quarter.
+int32_t batch_autotune(gr_batch* b) {
+  gr_context* c = b->ctx;
+  struct Cfg {
+    int shift, slice, waves;
+  };
+  const Cfg cands[] = {{5, 128, 1}, {5, 64, 1}, {5, 256, 1}, {5, 128, 2}, {4, 128, 1}, {4, 64, 1}, {4, 256, 1}, {4, 128, 2}};
+  Cfg best = cands[0];
+  float best_ms = 1e30f;
+  for (const Cfg& k : cands) {
+    c->tile_shift = k.shift;
+    c->slice_entries = (uint32_t)k.slice;
+    c->raster_waves = k.waves;
+    int32_t st = batch_run_plain(b, nullptr);  // warm up and size the buffers
+    if (st) return st;
+    float t = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      float ms = 0;
+      if ((st = batch_run_plain(b, &ms))) return st;
+      t = std::min(t, ms);
+    }
+    if (t < best_ms) {
+      best_ms = t;
+      best = k;
+    }
+  }
+  c->tile_shift = best.shift;
+  c->slice_entries = (uint32_t)best.slice;
+  c->raster_waves = best.waves;
+  int32_t st = batch_run_plain(b, nullptr);
+  if (st) return st;
+  const uint32_t want = std::max<uint32_t>(256, next_pow2((uint64_t)c->h_result->max_bin + c->h_result->max_bin / 4));
+  if (want != c->bin_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->bins);
+    dev_free(c->bin_count);
+    c->tiles_cap = 0;
+    c->bin_cap = 0;
+    c->want_bin_cap = want;
+  }
+  c->tuned_ms = best_ms;
+  return batch_run_plain(b, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gr_batch_create(gr_context* c, const gr_view* views, int32_t nviews, const gr_draw_item* items,
+                        int32_t nitems, int32_t autotune, gr_batch** out) {
+  if (!c || !out || nitems < 0 || (nitems > 0 && !items)) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  gr_batch* b = new (std::nothrow) gr_batch();
+  if (!b) return fail(GR_ERR_OUT_OF_MEMORY, "batch allocation");
+  b->ctx = c;
+  b->views.assign(views, views + std::max(nviews, 0));
+  b->items.assign(items, items + nitems);
+  int32_t st = views_in(c, b->views.data(), nviews, b->vin);
+  if (!st) st = autotune ? batch_autotune(b) : batch_run_plain(b, nullptr);
+  if (!st) st = batch_capture(b);
+  if (st) {
+    batch_drop_graph(b);
+    delete b;
+    return st;
+  }
+  *out = b;
+  return GR_OK;
+}
+
+int32_t gr_batch_run(gr_batch* b) {
+  if (!b) return fail(GR_ERR_INVALID_ARGUMENT, "batch is NULL");
+  gr_context* c = b->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  if (b->signature != buffers_signature(c)) {
+    // another draw on the context grew or moved a buffer the graph refers to
+    int32_t st = batch_capture(b);
+    if (st) return st;
+  }
+  CK(cudaGraphLaunch(b->exec, c->stream));
+  c->last_launches = b->launches;
+  return GR_OK;
+}
+
+int32_t gr_batch_sync(gr_batch* b) {
+  if (!b) return fail(GR_ERR_INVALID_ARGUMENT, "batch is NULL");
+  gr_context* c = b->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  int32_t err;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    if (!check_result(c, *c->h_result, &err)) return err;
+    if (err) return err;
+    // overflowed: buffers grow in prepare(); capture again and re-run
+    int32_t st = batch_capture(b);
+    if (st) return st;
+    CK(cudaGraphLaunch(b->exec, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return fail(GR_ERR_OUT_OF_MEMORY, "batch buffers kept overflowing after resizing");
+}
+
+int32_t gr_batch_tuning(gr_batch* b, int32_t* tile_size, int32_t* slice_entries, int32_t* raster_waves,
+                        int32_t* bin_capacity, float* tuned_ms) {
+  if (!b) return fail(GR_ERR_INVALID_ARGUMENT, "batch is NULL");
+  gr_context* c = b->ctx;
+  if (tile_size) *tile_size = 1 << c->tile_shift;
+  if (slice_entries) *slice_entries = (int32_t)c->slice_entries;
+  if (raster_waves) *raster_waves = c->raster_waves;
+  if (bin_capacity) *bin_capacity = (int32_t)c->bin_cap;
+  if (tuned_ms) *tuned_ms = c->tuned_ms;
+  return GR_OK;
+}
+
+int32_t gr_batch_destroy(gr_batch* b) {
+  if (!b) return GR_OK;
+  {
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    batch_drop_graph(b);
+    dev_free(b->d_views);
+    dev_free(b->d_items);
+  }
+  delete b;
+  return GR_OK;
 }
 
 int32_t gr_host_alloc(int64_t bytes, void** out) {
@@ -890,6 +1256,37 @@ int32_t gr_context_set_tuning(gr_context* c, int32_t tile_size, int32_t bin_capa
     c->want_bin_cap = (uint32_t)bin_capacity;
   }
   return GR_OK;
+}
+
+int32_t gr_context_set_raster(gr_context* c, int32_t slice_entries, int32_t raster_waves) {
+  if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  if (slice_entries < 0 || raster_waves < 0 || raster_waves > 16)
+    return fail(GR_ERR_INVALID_ARGUMENT, "bad raster tuning");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (slice_entries) c->slice_entries = (uint32_t)slice_entries;
+  if (raster_waves) c->raster_waves = raster_waves;
+  return GR_OK;
+}
+
+int32_t gr_context_autotune(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p) {
+  if (!c || !p) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  int32_t st;
+  const size_t px = (size_t)p->width * (size_t)p->height;
+  if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
+  if ((st = ensure_fb(c, px))) return st;
+  gr_batch b;
+  b.ctx = c;
+  gr_view v;
+  v.params = *p;
+  v.rgba_dev = (uint8_t*)c->fb_rgba;
+  v.z_dev = c->fb_z;
+  b.views.push_back(v);
+  b.vin.push_back(ViewIn{&b.views[0].params, c->fb_rgba, c->fb_z});
+  if (n > 0) b.items.assign(items, items + n);
+  for (auto& it : b.items) it.reserved = 0;
+  return batch_autotune(&b);
 }
 
 int32_t gr_context_get_tuning(gr_context* c, int32_t* tile_size, int32_t* bin_capacity) {

@@ -29,6 +29,21 @@ struct DevTex {
   const uint32_t* px;   // RGBA8 texels, row-major
 };
 
+// One view of a frame or batch: framebuffer, renderer flags, screen matrix,
+// light and its range of raster tiles.
+struct DevView {
+  int W, H;
+  uint32_t flags;                   // GR_* renderer flags
+  int tiles_x, tiles_y;
+  uint32_t tile_base;               // first global raster tile of this view
+  int vec_ok;                       // outputs allow 16-byte vector stores
+  int pad;
+  float S[8];                       // screen matrix rows 0 and 1
+  float L[4];                       // light direction (L[3] unused)
+  uint32_t* out_rgba;               // H x W RGBA8
+  float* out_z;                     // H x W
+};
+
 // One draw item in device memory: an Object with its matrices.
 struct DevItem {
   float mvp[16];
@@ -47,7 +62,7 @@ struct DevItem {
   int block_base;                   // first k_project block of this item
   int light_base;                   // first entry of this item in FrameArgs::vlight
   int light_block_base;             // first k_light block of this item
-  int pad;
+  int view;                         // index into FrameArgs::views
 };
 
 // Raster setup of one binned triangle (64 bytes).  For "narrow" triangles
@@ -95,18 +110,22 @@ struct DevWork {
   unsigned int error;               // bit 0 clip overflow, bit 1 bad normal index
   unsigned int nclip;               // faces queued for the general clipper
   unsigned int clip_need;
+  unsigned int max_bin;             // largest tile bin of the frame (k_plan)
+  unsigned int plan_front, plan_back;  // raster work items: split tiles, whole tiles
+  unsigned int raster_next, raster_exit;  // persistent raster: next item, finished CTAs
 };
 
 struct DevResult {
-  unsigned long long tpf;
-  unsigned int nrec, nbig, bin_need, rec_need, big_need, error, nclip, clip_need;
+  unsigned long long tpf;           // binned triangles over all views
+  unsigned int nrec, nbig, bin_need, rec_need, big_need, error, nclip, clip_need, max_bin, items;
 };
 
 // Everything a frame's kernels need, passed by value.
 struct FrameArgs {
-  int W, H;
-  uint32_t flags;
-  int tiles_x, tiles_y;
+  const DevView* views;
+  int num_views;
+  uint32_t total_tiles;             // sum of the views' tiles
+  uint32_t flags_any;               // OR of the views' flags
   int tile_shift;                   // raster tile = (1 << tile_shift)^2 pixels (4 or 5)
   int num_items;
   int total_blocks;
@@ -114,9 +133,6 @@ struct FrameArgs {
   uint32_t rec_cap;
   uint32_t big_cap;
   uint32_t key_cap;
-  int vec_ok;                       // outputs allow 16-byte vector stores
-  float S[8];                       // screen matrix rows 0 and 1
-  float L[3];                       // light direction
   const DevItem* items;
   const DevTex* texs;
   int num_tex;
@@ -127,7 +143,7 @@ struct FrameArgs {
   uint32_t* rec_of_key;             // order key -> record index
   uint32_t* bins;                   // tiles x bin_cap record indices
   uint32_t* bin_count;              // per tile
-  uint32_t* big;                    // multi-tile record queue
+  uint2* big;                       // multi-tile queue: (record, view)
   uint2* clip;                      // (item, face) pairs for the general clipper
   uint32_t clip_cap;
   float* vlight;                    // per-normal Gouraud intensities (k_light)
@@ -137,14 +153,20 @@ struct FrameArgs {
   uint32_t slice_entries;           // bin entries per slice
   DevWork* work;
   DevResult* result;
-  uint32_t* out_rgba;               // H x W RGBA8
-  float* out_z;                     // H x W
+  unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)
+  unsigned long long* view_tpf_out; // per view: published by k_plan
+  uint2* plan;                      // raster work items (tile, slice), plan_cap entries
+  uint32_t plan_cap;
+  int raster_ctas;                  // persistent raster grid
 };
 
 // Kernel launchers (gr_kernels.cu).
 // events (optional): 4 cudaEvent_t recorded before k_project, after k_project,
 // after k_bin_big and after k_raster.
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events);
+
+// Persistent raster grid: SMs x resident CTAs of k_raster<TS> x waves.
+int raster_grid(int tile_shift, int waves);
 
 // Records a message for gr_last_error() on this thread and returns code (gr_api.cpp).
 int32_t set_error(int32_t code, const char* fmt, ...);

@@ -298,7 +298,8 @@ __device__ __forceinline__ float light_of(const float* world, V4 nrm, const floa
 }
 
 __device__ __forceinline__ bool gouraud(const FrameArgs& a, const DevItem& it) {
-  return (a.flags & 0x08u) && !(a.flags & 0x10u) && it.nn != 0;
+  const uint32_t fl = a.views[it.view].flags;
+  return (fl & 0x08u) && !(fl & 0x10u) && it.nn != 0;
 }
 
 // facingCamera (renderer.go:246-250) on clip-space vertices.
@@ -315,7 +316,8 @@ __device__ __forceinline__ bool facing_camera(V4 v0, V4 v1, V4 v2) {
 // Per-vertex attributes of face f (intensity, UV, RGB) and its texture slot.
 __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevItem& it, int f, int i0, int i1, int i2,
                                                 const float* world, PV& p0, PV& p1, PV& p2, int& tex) {
-  const uint32_t fl = a.flags;
+  const DevView& vw = a.views[it.view];
+  const uint32_t fl = vw.flags;
   float in0, in1, in2;
   if (fl & 0x08u) {
     if (gouraud(a, it)) {
@@ -325,7 +327,7 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
       in1 = __ldg(vl + __ldg(it.nidx + 3 * f + 1));
       in2 = __ldg(vl + __ldg(it.nidx + 3 * f + 2));
     } else {
-      in0 = in1 = in2 = light_of(world, ld4(it.fnrm + 4 * (size_t)f), a.L);
+      in0 = in1 = in2 = light_of(world, ld4(it.fnrm + 4 * (size_t)f), vw.L);
     }
   } else {
     in0 = in1 = in2 = 0.5f;
@@ -385,19 +387,20 @@ __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Set
 }
 
 // Binning without warp aggregation (the rare clipped path).
-__device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const TriRaster& t) {
+__device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const TriRaster& t, int view) {
+  const DevView& vw = a.views[view];
   const uint32_t tx0 = (uint32_t)t.bx0 >> a.tile_shift, tx1 = (uint32_t)t.bx1 >> a.tile_shift;
   const uint32_t ty0 = (uint32_t)t.by0 >> a.tile_shift, ty1 = (uint32_t)t.by1 >> a.tile_shift;
   const uint32_t ntiles = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
   if (ntiles <= (uint32_t)kBinDirectMax) {
     for (uint32_t ty = ty0; ty <= ty1; ++ty)
       for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
+        const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
         bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
       }
   } else {
     const uint32_t q = atomicAdd(&a.work->nbig, 1u);
-    if (q < a.big_cap) a.big[q] = r;
+    if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)view);
     else atomicMax(&a.work->big_need, q + 1);
   }
 }
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
   __syncthreads();
   if (!gouraud(a, it)) return;
   const int n = ((int)blockIdx.x - it.light_block_base) * 256 + (int)threadIdx.x;
-  if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.L);
+  if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.views[it.view].L);
 }
 
 // ---------------------------------------------------------------------------
@@ -438,6 +441,7 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
+  __shared__ float s_S[8];
   __shared__ int s_item;
   __shared__ int s_vis;
   __shared__ unsigned s_out[8];
@@ -447,10 +451,12 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   __syncthreads();
   const int item = s_item;
   const DevItem& it = a.items[item];
+  const DevView& vw = a.views[it.view];
   if (tid < 16) {
     s_mvp[tid] = it.mvp[tid];
     s_world[tid] = it.world[tid];
   }
+  if (tid < 8) s_S[tid] = vw.S[tid];
   __syncthreads();
   // Frustum.BoxVisibility of the transformed bounding box (renderer.go:268-275).
   if (tid < 8) {
@@ -477,7 +483,8 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   const int vis = s_vis;
   if (vis == 0) return;  // whole block: object outside the frustum
 
-  const uint32_t fl = a.flags;
+  const uint32_t fl = vw.flags;
+  const int W = vw.W, H = vw.H;
   const int f = ((int)blockIdx.x - it.block_base) * kProjectThreads + tid;
   const bool valid = f < it.nf;
   const unsigned lane = lane_id();
@@ -512,14 +519,14 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
       PV p0, p1, p2;
       p0.p = v0; p1.p = v1; p2.p = v2;
       face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
-      s0 = to_screen(p0, a.S);
-      s1 = to_screen(p1, a.S);
-      s2 = to_screen(p2, a.S);
-      if (bin_test(s0, s1, s2, (float)a.W, (float)a.H)) {
+      s0 = to_screen(p0, s_S);
+      s1 = to_screen(p1, s_S);
+      s2 = to_screen(p2, s_S);
+      if (bin_test(s0, s1, s2, (float)W, (float)H)) {
         ntpf = 1;
         Setup s;
         // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
-        emit = (fl & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s);
+        emit = (fl & 0x02u) && setup_tri(s0, s1, s2, W, H, s);
       }
     }
   }
@@ -538,9 +545,9 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
     }
   }
 
-  // TPF: one atomic per warp.
+  // TPF: one atomic per warp (all faces of a block belong to one view).
   const int wt = __reduce_add_sync(FULL_MASK, ntpf);
-  if (lane == 0 && wt) atomicAdd(&a.work->tpf, (unsigned long long)wt);
+  if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
 
   // Compact records: one atomic per warp, lane offsets from the ballot.
   const unsigned em = __ballot_sync(FULL_MASK, emit);
@@ -557,7 +564,7 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
   if (ok) {
     Setup s;
-    setup_tri(s0, s1, s2, a.W, a.H, s);
+    setup_tri(s0, s1, s2, W, H, s);
     write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
     tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
     tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
@@ -569,7 +576,7 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   const bool one = ntiles == 1;
   const unsigned m1 = __ballot_sync(FULL_MASK, one);
   if (one) {
-    const uint32_t tile = ty0 * (uint32_t)a.tiles_x + tx0;
+    const uint32_t tile = vw.tile_base + ty0 * (uint32_t)vw.tiles_x + tx0;
     const unsigned grp = __match_any_sync(m1, tile);
     const int leader = __ffs(grp) - 1;
     const unsigned rank = __popc(grp & ((1u << lane) - 1u));
@@ -582,7 +589,7 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
     for (uint32_t ty = ty0; ty <= ty1; ++ty)
       for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
+        const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
         bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
       }
   }
@@ -596,7 +603,7 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
     qb = __shfl_sync(FULL_MASK, qb, l2);
     if (many) {
       const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
-      if (q < a.big_cap) a.big[q] = r;
+      if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)it.view);
       else atomicMax(&a.work->big_need, q + 1);
     }
   }
@@ -707,26 +714,27 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
       continue;
     }
     if (count < 3) continue;  // Polygon.Triangulate returns nothing
-    const SV sv = to_screen(v, a.S);  // lane k: polygon vertex k
+    const DevView& vw = a.views[it.view];
+    const SV sv = to_screen(v, vw.S);  // lane k: polygon vertex k
     const SV s0 = shfl_sv(sv, 0), s1 = shfl_sv(sv, lane + 1 < 9 ? lane + 1 : 0),
              s2 = shfl_sv(sv, lane + 2 < 9 ? lane + 2 : 0);
     const bool fan = lane + 2 < count;
     int ntpf = 0;
-    if (fan && bin_test(s0, s1, s2, (float)a.W, (float)a.H)) {
+    if (fan && bin_test(s0, s1, s2, (float)vw.W, (float)vw.H)) {
       ntpf = 1;
       Setup s;
-      if ((a.flags & 0x02u) && setup_tri(s0, s1, s2, a.W, a.H, s)) {
+      if ((vw.flags & 0x02u) && setup_tri(s0, s1, s2, vw.W, vw.H, s)) {
         const uint32_t r = atomicAdd(&a.work->nrec, 1u);
         if (r < a.rec_cap) {
           write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
-          bin_record(a, r, s.r);
+          bin_record(a, r, s.r, it.view);
         } else {
           atomicMax(&a.work->rec_need, r + 1);
         }
       }
     }
     const int wt = __reduce_add_sync(FULL_MASK, ntpf);
-    if (lane == 0 && wt) atomicAdd(&a.work->tpf, (unsigned long long)wt);
+    if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
   }
 }
 
@@ -738,7 +746,9 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
   const int ts = 1 << sh;
   const uint32_t nbig = min(*(volatile uint32_t*)&a.work->nbig, a.big_cap);
   for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
-    const uint32_t r = a.big[q];
+    const uint2 be = a.big[q];
+    const uint32_t r = be.x;
+    const DevView& vw = a.views[be.y];
     const TriRaster t = a.rast[r];
     const uint32_t tx0 = (uint32_t)t.bx0 >> sh, tx1 = (uint32_t)t.bx1 >> sh;
     const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
@@ -758,7 +768,7 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
         const int e20 = t.c20 + min(t.a20 * X0, t.a20 * X1) + min(t.b20 * Y0, t.b20 * Y1);
         if (e01 >= 0 || e12 >= 0 || e20 >= 0) continue;
       }
-      const uint32_t tile = ty * (uint32_t)a.tiles_x + tx;
+      const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
       bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
     }
   }
@@ -931,57 +941,61 @@ __device__ __forceinline__ void walk_blocks(CandQueue<TS>& q, unsigned long long
   }
 }
 
+// Number of raster slices of a tile holding n bin entries.
+__device__ __forceinline__ uint32_t tile_slices(const FrameArgs& a, uint32_t n) {
+  return min((uint32_t)kRasterMaxSlices, max(1u, (n + a.slice_entries - 1) / a.slice_entries));
+}
+
 template <int TS>
-__global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const FrameArgs a) {
+struct RasterSmem {
+  static constexpr int kWarps = RasterShape<TS>::kWarps;
+  static constexpr uint32_t kLargeCap = 128;  // queued large triangles per round
+  static constexpr int kSlots = 64;           // triangle table: 32 lane slots + 32 for large ones
+  __align__(16) unsigned long long skey[TS * RasterShape<TS>::kStride];
+  __align__(16) TriRaster tri[kWarps][kSlots];
+  uint32_t trec[kWarps][kSlots];
+  uint32_t ent[kWarps][64];
+  uint32_t large[kLargeCap + RasterShape<TS>::kThreads];
+  uint32_t next, nlarge, last;
+};
+
+// One raster work item: slice `slice` of global tile `tile` of view `view`.
+template <int TS>
+__device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, uint32_t slice, int view,
+                                            RasterSmem<TS>& sm) {
   constexpr int kThreads = RasterShape<TS>::kThreads;
   constexpr int kStride = RasterShape<TS>::kStride;
   constexpr int kWarps = RasterShape<TS>::kWarps;
-  constexpr uint32_t kLargeCap = 128;     // queued large triangles per round
+  constexpr uint32_t kLargeCap = RasterSmem<TS>::kLargeCap;
   constexpr int kLaneArea = 256;          // footprints up to 256 pixels: one lane each
-  constexpr int kSlots = 64;              // triangle table: 32 lane slots + 32 for large ones
-  constexpr uint32_t kMaxSlices = kRasterMaxSlices;
-  __shared__ __align__(16) unsigned long long skey[TS * kStride];
-  __shared__ __align__(16) TriRaster s_tri[kWarps][kSlots];
-  __shared__ uint32_t s_trec[kWarps][kSlots];
-  __shared__ uint32_t s_ent[kWarps][64];
-  __shared__ uint32_t s_large[kLargeCap + kThreads];
-  __shared__ uint32_t s_next, s_nlarge, s_last;
+  unsigned long long* skey = sm.skey;
+  auto& s_tri = sm.tri;
+  auto& s_trec = sm.trec;
+  auto& s_ent = sm.ent;
+  uint32_t* s_large = sm.large;
+  uint32_t& s_next = sm.next;
+  uint32_t& s_nlarge = sm.nlarge;
+  uint32_t& s_last = sm.last;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
-  // A tile's bin is split into up to kMaxSlices slices, one CTA each; CTAs of
-  // one tile are adjacent in launch order.
-  const uint32_t tile = blockIdx.x / kMaxSlices;
-  const uint32_t slice = blockIdx.x % kMaxSlices;
+  const DevView& vw = a.views[view];
+  // A tile's bin is split into up to kRasterMaxSlices slices, one work item each.
   const uint32_t count = a.bin_count[tile];
   const uint32_t n = min(count, a.bin_cap);
-  const uint32_t nslices = min((uint32_t)kMaxSlices, max(1u, (n + a.slice_entries - 1) / a.slice_entries));
-  if (slice >= nslices) return;  // whole CTA: this tile needs fewer slices
+  const uint32_t nslices = tile_slices(a, n);
+  if (slice >= nslices) return;
   const uint32_t per = (((n + nslices - 1) / nslices) + 31u) & ~31u;
   const uint32_t lo = min(n, slice * per), hi = min(n, lo + per);
-  const int tx0 = (int)(tile % (uint32_t)a.tiles_x) * TS;
-  const int ty0 = (int)(tile / (uint32_t)a.tiles_x) * TS;
-  const int tx1 = min(tx0 + TS - 1, a.W - 1);
-  const int ty1 = min(ty0 + TS - 1, a.H - 1);
+  const uint32_t lt = tile - vw.tile_base;
+  const int tx0 = (int)(lt % (uint32_t)vw.tiles_x) * TS;
+  const int ty0 = (int)(lt / (uint32_t)vw.tiles_x) * TS;
+  const int tx1 = min(tx0 + TS - 1, vw.W - 1);
+  const int ty1 = min(ty0 + TS - 1, vw.H - 1);
 
   for (int i = tid; i < TS * kStride; i += kThreads) skey[i] = BG_KEY;
   if (tid == 0) {
     s_next = lo;
     s_nlarge = 0;
-  }
-  if (tid == 0 && blockIdx.x == 0) {
-    // publish and reset the frame counters (all appends are complete)
-    DevWork* w = a.work;
-    a.result->tpf = w->tpf;
-    a.result->nrec = w->nrec;
-    a.result->nbig = w->nbig;
-    a.result->bin_need = w->bin_need;
-    a.result->rec_need = w->rec_need;
-    a.result->big_need = w->big_need;
-    a.result->error = w->error;
-    a.result->nclip = w->nclip;
-    a.result->clip_need = w->clip_need;
-    w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
-    w->nclip = 0; w->clip_need = 0;
   }
   __syncthreads();
 
@@ -1190,18 +1204,132 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const Fram
       out_z[j] = z;
     }
     const int x = tx0 + col;
-    const size_t o = (size_t)y * (size_t)a.W + (size_t)x;
-    if (a.vec_ok && x + 3 <= tx1) {
-      *reinterpret_cast<uint4*>(a.out_rgba + o) = make_uint4(out_c[0], out_c[1], out_c[2], out_c[3]);
-      *reinterpret_cast<float4*>(a.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
+    const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
+    if (vw.vec_ok && x + 3 <= tx1) {
+      *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(out_c[0], out_c[1], out_c[2], out_c[3]);
+      *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
     } else {
       for (int j = 0; j < 4 && x + j <= tx1; ++j) {
-        a.out_rgba[o + j] = out_c[j];
-        a.out_z[o + j] = out_z[j];
+        vw.out_rgba[o + j] = out_c[j];
+        vw.out_z[o + j] = out_z[j];
       }
     }
   }
   if (tid == 0) a.bin_count[tile] = 0;  // ready for the next frame
+}
+
+// ---------------------------------------------------------------------------
+// k_plan: the raster work queue.  One thread per global tile: a tile whose
+// bin needs several slices contributes one item per slice to the front of
+// the queue (heavy tiles start first), any other tile one item to the back.
+// One atomic per CTA reserves each part; no ordering between CTAs is needed.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
+  __shared__ uint32_t s_nf, s_nb, s_bf, s_bb, s_max;
+  const uint32_t tile = blockIdx.x * 256u + threadIdx.x;
+  if (threadIdx.x == 0) {
+    s_nf = 0;
+    s_nb = 0;
+    s_max = 0;
+  }
+  __syncthreads();
+  const bool valid = tile < a.total_tiles;
+  const uint32_t count = valid ? a.bin_count[tile] : 0u;
+  const uint32_t ns = valid ? tile_slices(a, min(count, a.bin_cap)) : 0u;
+  uint32_t mf = 0, mb = 0;
+  if (valid) {
+    atomicMax(&s_max, count);
+    if (ns > 1) mf = atomicAdd(&s_nf, ns);
+    else mb = atomicAdd(&s_nb, 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_bf = s_nf ? atomicAdd(&a.work->plan_front, s_nf) : 0u;
+    s_bb = s_nb ? atomicAdd(&a.work->plan_back, s_nb) : 0u;
+    if (s_max) atomicMax(&a.work->max_bin, s_max);
+  }
+  __syncthreads();
+  if (!valid) return;
+  if (ns > 1) {
+    for (uint32_t k = 0; k < ns; ++k) a.plan[s_bf + mf + k] = make_uint2(tile, k);
+  } else {
+    a.plan[a.plan_cap - 1u - (s_bb + mb)] = make_uint2(tile, 0u);
+  }
+}
+
+// Persistent raster: CTAs take work items from the queue until it is empty;
+// the last CTA to finish publishes and resets the frame's counters.
+template <int TS>
+__global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const FrameArgs a) {
+  __shared__ RasterSmem<TS> sm;
+  __shared__ uint32_t s_item, s_tile, s_slice, s_lastcta;
+  __shared__ int s_view;
+  const uint32_t front = *(volatile uint32_t*)&a.work->plan_front;
+  const uint32_t total = front + *(volatile uint32_t*)&a.work->plan_back;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t i = atomicAdd(&a.work->raster_next, 1u);
+      s_item = i;
+      if (i < total) {
+        const uint2 w = i < front ? a.plan[i] : a.plan[a.plan_cap - 1u - (i - front)];
+        s_tile = w.x;
+        s_slice = w.y;
+        int lo = 0, hi = a.num_views - 1;  // last view whose first tile <= w.x
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (a.views[mid].tile_base <= w.x) lo = mid; else hi = mid - 1;
+        }
+        s_view = lo;
+      }
+    }
+    __syncthreads();
+    if (s_item >= total) break;
+    raster_item<TS>(a, s_tile, s_slice, s_view, sm);
+    __syncthreads();  // shared memory is reused by the next item
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_lastcta = atomicAdd(&a.work->raster_exit, 1u) == gridDim.x - 1 ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!s_lastcta) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    DevWork* w = a.work;
+    DevResult* r = a.result;
+    r->tpf = 0;
+    r->nrec = w->nrec;
+    r->nbig = w->nbig;
+    r->bin_need = w->bin_need;
+    r->rec_need = w->rec_need;
+    r->big_need = w->big_need;
+    r->error = w->error;
+    r->nclip = w->nclip;
+    r->clip_need = w->clip_need;
+    r->max_bin = w->max_bin;
+    r->items = total;
+    w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
+    w->nclip = 0; w->clip_need = 0; w->max_bin = 0;
+    w->plan_front = 0; w->plan_back = 0; w->raster_next = 0; w->raster_exit = 0;
+  }
+  __syncthreads();
+  for (int v = threadIdx.x; v < a.num_views; v += blockDim.x) {
+    const unsigned long long t = a.view_tpf[v];
+    a.view_tpf_out[v] = t;
+    a.view_tpf[v] = 0ull;
+    if (t) atomicAdd(&a.result->tpf, t);
+  }
+}
+
+int raster_grid(int tile_shift, int waves) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (tile_shift == 4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<16>, RasterShape<16>::kThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<32>, RasterShape<32>::kThreads, 0);
+  return max(1, sms) * max(1, per) * max(1, waves);
 }
 
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events) {
@@ -1216,7 +1344,7 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     k_project<<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
-    if (a.flags & 0x01u) {
+    if (a.flags_any & 0x01u) {
       k_clip<<<kClipBlocks, 128, 0, s>>>(a);
       ++n;
     }
@@ -1227,11 +1355,12 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     cudaEventRecord((cudaEvent_t)events[1], s);
     cudaEventRecord((cudaEvent_t)events[2], s);
   }
-  const int tiles = a.tiles_x * a.tiles_y;
+  k_plan<<<(a.total_tiles + 255) / 256, 256, 0, s>>>(a);
+  ++n;
   if (a.tile_shift == 4)
-    k_raster<16><<<tiles * kRasterMaxSlices, RasterShape<16>::kThreads, 0, s>>>(a);
+    k_raster<16><<<a.raster_ctas, RasterShape<16>::kThreads, 0, s>>>(a);
   else
-    k_raster<32><<<tiles * kRasterMaxSlices, RasterShape<32>::kThreads, 0, s>>>(a);
+    k_raster<32><<<a.raster_ctas, RasterShape<32>::kThreads, 0, s>>>(a);
   ++n;
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
   if (launches) *launches = n;

@@ -49,14 +49,14 @@ constexpr uint32_t kBinCap = 1024;
 constexpr uint32_t kQueueCap = kMaxFaces + 1024;
 constexpr size_t kScratchBytes = 8u << 20;
 
-__device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
-  size_t items, texs, rast, shade, wide, tcol, keys, bins, bin_count, big, clip, vlight, gkey, tile_done, work,
-      result, end;
+  size_t items, texs, views, view_tpf, view_tpf_out, plan, rast, shade, wide, tcol, keys, bins, bin_count, big, clip,
+      vlight, gkey, tile_done, work, result, end;
 };
 
 constexpr Layout make_layout() {
@@ -64,6 +64,10 @@ constexpr Layout make_layout() {
   size_t o = 0;
   l.items = o; o += up256(sizeof(DevItem) * kMaxObjects);
   l.texs = o; o += up256(sizeof(DevTex) * kMaxTextures);
+  l.views = o; o += up256(sizeof(DevView));
+  l.view_tpf = o; o += up256(sizeof(unsigned long long));
+  l.view_tpf_out = o; o += up256(sizeof(unsigned long long));
+  l.plan = o; o += up256(sizeof(uint2) * kTiles * kRasterMaxSlices);
   l.rast = o; o += up256(sizeof(TriRaster) * kRecCap);
   l.shade = o; o += up256(sizeof(TriShade) * kRecCap);
   l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
@@ -71,7 +75,7 @@ constexpr Layout make_layout() {
   l.keys = o; o += up256(sizeof(uint32_t) * kKeyCap);
   l.bins = o; o += up256(sizeof(uint32_t) * kTiles * kBinCap);
   l.bin_count = o; o += up256(sizeof(uint32_t) * kTiles);
-  l.big = o; o += up256(sizeof(uint32_t) * kQueueCap);
+  l.big = o; o += up256(sizeof(uint2) * kQueueCap);
   l.clip = o; o += up256(sizeof(uint2) * kQueueCap);
   l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
   l.gkey = o; o += up256(sizeof(unsigned long long) * kTiles * 1024);
@@ -166,6 +170,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     d.nv = m.num_vertices; d.nn = m.vertex_normals ? m.num_normals : 0; d.nf = m.num_faces;
     d.face_base = fb;
     d.block_base = blocks;
+    d.view = 0;
     blocks += (m.num_faces + kProjectThreads - 1) / kProjectThreads;
     d.light_base = light_total;
     d.light_block_base = light_blocks;
@@ -196,14 +201,28 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     }
   }
 
+  DevView view;
+  std::memset(&view, 0, sizeof(view));
+  view.W = p->width;
+  view.H = p->height;
+  view.flags = p->flags;
+  view.tiles_x = (p->width + 31) / 32;
+  view.tiles_y = (p->height + 31) / 32;
+  view.tile_base = 0;
+  for (int k = 0; k < 8; ++k) view.S[k] = p->screen[k];
+  for (int k = 0; k < 3; ++k) view.L[k] = p->light[k];
+  view.out_rgba = (uint32_t*)rgba_dev;
+  view.out_z = z_dev;
+  view.vec_ok = (p->width % 4 == 0) && ((uintptr_t)rgba_dev % 16 == 0) && ((uintptr_t)z_dev % 16 == 0);
+  const int tiles = view.tiles_x * view.tiles_y;
+
   FrameArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.W = p->width;
-  a.H = p->height;
-  a.flags = p->flags;
+  a.views = (const DevView*)(base + kLayout.views);
+  a.num_views = 1;
+  a.total_tiles = (uint32_t)tiles;
+  a.flags_any = p->flags;
   a.tile_shift = 5;
-  a.tiles_x = (p->width + 31) / 32;
-  a.tiles_y = (p->height + 31) / 32;
   a.num_items = live;
   a.total_blocks = blocks;
   a.bin_cap = kBinCap;
@@ -213,8 +232,6 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.clip_cap = kQueueCap;
   a.slice_entries = kDefaultSliceEntries;
   a.light_blocks = light_blocks;
-  for (int k = 0; k < 8; ++k) a.S[k] = p->screen[k];
-  for (int k = 0; k < 3; ++k) a.L[k] = p->light[k];
   a.items = (const DevItem*)(base + kLayout.items);
   a.texs = (const DevTex*)(base + kLayout.texs);
   a.num_tex = num_textures;
@@ -225,24 +242,27 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.rec_of_key = (uint32_t*)(base + kLayout.keys);
   a.bins = (uint32_t*)(base + kLayout.bins);
   a.bin_count = (uint32_t*)(base + kLayout.bin_count);
-  a.big = (uint32_t*)(base + kLayout.big);
+  a.big = (uint2*)(base + kLayout.big);
   a.clip = (uint2*)(base + kLayout.clip);
   a.vlight = (float*)(base + kLayout.vlight);
   a.gkey = (unsigned long long*)(base + kLayout.gkey);
   a.tile_done = (uint32_t*)(base + kLayout.tile_done);
   a.work = (DevWork*)(base + kLayout.work);
   a.result = (DevResult*)(base + kLayout.result);
-  a.out_rgba = (uint32_t*)rgba_dev;
-  a.out_z = z_dev;
-  a.vec_ok = (p->width % 4 == 0) && ((uintptr_t)rgba_dev % 16 == 0) && ((uintptr_t)z_dev % 16 == 0);
+  a.view_tpf = (unsigned long long*)(base + kLayout.view_tpf);
+  a.view_tpf_out = (unsigned long long*)(base + kLayout.view_tpf_out);
+  a.plan = (uint2*)(base + kLayout.plan);
+  a.plan_cap = (uint32_t)(kTiles * kRasterMaxSlices);
+  a.raster_ctas = raster_grid(5, 1);
 
   // The array keeps the previous call's contents: zero what the kernels
   // expect to find zeroed (counters, bin counts, split-tile keys).
-  const int tiles = a.tiles_x * a.tiles_y;
   e = cudaMemsetAsync(base + kLayout.bin_count, 0, sizeof(uint32_t) * tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.gkey, 0, sizeof(unsigned long long) * tiles * 1024, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.tile_done, 0, sizeof(uint32_t) * tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.work, 0, sizeof(DevWork), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.view_tpf, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base + kLayout.views, &view, sizeof(view), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && live) e = cudaMemcpyAsync(base + kLayout.items, items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && num_textures)
     e = cudaMemcpyAsync(base + kLayout.texs, texs, sizeof(DevTex) * num_textures, cudaMemcpyHostToDevice, s);

@@ -104,6 +104,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
+        self._batches = []  # closed before the context: a batch must not outlive it
         N.check(N.lib().gr_context_create(device, C.byref(self._h)))
 
     @property
@@ -111,6 +112,9 @@ class Context:
         return self._h
 
     def close(self):
+        for b in self._batches:
+            b.close()
+        self._batches = []
         if self._h:
             N.lib().gr_context_destroy(self._h)
             self._h = C.c_void_p()
@@ -363,3 +367,71 @@ class UploadedScene:
         z = np.empty((self.scene.height, self.scene.width), np.float32)
         tpf = self.draw(rgba, z)
         return rgba, z, tpf
+
+
+# ---- batched multi-view ----
+
+class Batch:
+    """A fixed set of views rendered by one CUDA graph (gr_batch_*).
+
+    ``views`` is a list of (FrameParams, rgba device pointer, z device pointer);
+    ``entries`` a list of (mesh handle, mvp, world, view index).
+    """
+
+    def __init__(self, ctx: Context, views, entries, autotune: bool = True):
+        self.ctx = ctx
+        self._views = (N.View * len(views))()
+        for i, (params, rgba, z) in enumerate(views):
+            self._views[i].params = params
+            self._views[i].rgba_dev = int(rgba)
+            self._views[i].z_dev = int(z)
+        self._items = make_items([(m, mvp, w) for m, mvp, w, _ in entries])
+        for i, (_, _, _, v) in enumerate(entries):
+            self._items[i].reserved = v
+        self.nviews = len(views)
+        self._h = C.c_void_p()
+        N.check(N.lib().gr_batch_create(ctx.handle, self._views, len(views), self._items, len(entries),
+                                        1 if autotune else 0, C.byref(self._h)))
+        ctx._batches.append(self)
+
+    def run(self):
+        N.check(N.lib().gr_batch_run(self._h))
+
+    def sync(self):
+        N.check(N.lib().gr_batch_sync(self._h))
+
+    def tuning(self):
+        t, s, w, b = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        ms = C.c_float()
+        N.check(N.lib().gr_batch_tuning(self._h, C.byref(t), C.byref(s), C.byref(w), C.byref(b), C.byref(ms)))
+        return {"tile_size": t.value, "slice_entries": s.value, "raster_waves": w.value,
+                "bin_capacity": b.value, "tuned_ms": ms.value}
+
+    def view_tpf(self):
+        out = (C.c_int64 * self.nviews)()
+        N.check(N.lib().gr_context_view_tpf(self.ctx.handle, out, self.nviews))
+        return list(out)
+
+    def close(self):
+        if self._h:
+            N.lib().gr_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def draw_views(ctx: Context, views, entries) -> None:
+    """gr_draw_views: views = [(FrameParams, rgba_dev, z_dev)], entries = [(mesh, mvp, world, view)]."""
+    vs = (N.View * len(views))()
+    for i, (params, rgba, z) in enumerate(views):
+        vs[i].params = params
+        vs[i].rgba_dev = int(rgba)
+        vs[i].z_dev = int(z)
+    items = make_items([(m, mvp, w) for m, mvp, w, _ in entries])
+    for i, (_, _, _, v) in enumerate(entries):
+        items[i].reserved = v
+    N.check(N.lib().gr_draw_views(ctx.handle, vs, len(views), items, len(entries)))

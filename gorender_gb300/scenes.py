@@ -391,3 +391,59 @@ def scene_icospheres_1920x1080(count: int = 64, seed: int = 0, levels=(5, 6)) ->
         objs.append(ObjectData(mesh, scale=(s, s, s), translation=(float(p[0]), float(p[1]), float(p[2]) - 30.0)))
     cam = CameraData((0.0, 0.0, 0.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0))
     return SceneData(f"icospheres{count}-1920x1080", 1920, 1080, objs, cam, [], DEFAULT_FLAGS)
+
+
+@dataclasses.dataclass
+class ViewSpec:
+    """One view of a multi-view batch: its scene (objects, camera, size, flags)."""
+
+    scene: SceneData
+
+
+def multiview_batch(count: int = 256, seed: int = 0, min_tris: int = 100, max_tris: int = 200_000,
+                    resolutions=((256, 256), (512, 512), (640, 360), (1280, 720))) -> List[SceneData]:
+    """Views with their own mesh each: triangle counts log-uniform in
+    [min_tris, max_tris] (heightfields and icospheres alternate), camera on a
+    sphere of radius U[2.5, 6] looking at the origin, resolution drawn from
+    ``resolutions``, material cycling through flat, Gouraud and
+    perspective-textured (seeded 16x16 RGBA8)."""
+    rng = SplitMix64(seed)
+    out = []
+    logs = rng.uniform(count, math.log(min_tris), math.log(max_tris)).astype(np.float64)
+    radii = rng.uniform(count, 2.5, 6.0).astype(np.float64)
+    dirs = rng.uniform(3 * count, -1.0, 1.0).astype(np.float64).reshape(count, 3)
+    res_idx = rng.integers(count, 0, len(resolutions))
+    for k in range(count):
+        target = int(round(math.exp(logs[k])))
+        material = k % 3  # 0 flat, 1 Gouraud, 2 textured
+        if k % 2 == 0:
+            n = max(3, int(round(math.sqrt(target / 2.0))) + 1)
+            m = heightfield(n, extent=1.5, amp=0.1, seed=seed * 7919 + k, uv=(material == 2))
+            if material == 1:
+                # smooth-ish vertex normals pointing up for Gouraud lighting
+                vn = np.zeros((m.nv, 4), np.float32)
+                vn[:, 1] = 1.0
+                vn[:, 3] = 1.0
+                m.vnrm = vn
+                m.nidx = m.vidx.copy()
+        else:
+            level = int(min(6, max(1, round(math.log(max(target, 20) / 20.0, 4)))))
+            m = icosphere(level, noise=0.05, seed=seed * 7919 + k, normals=(material == 1))
+            if material == 2:
+                # spherical corner UVs
+                p = m.pos[m.vidx.reshape(-1), :3].astype(np.float64)
+                u = (np.arctan2(p[:, 2], p[:, 0]) / (2 * math.pi) + 0.5).astype(np.float32)
+                v = (p[:, 1] * 0.5 + 0.5).astype(np.float32)
+                m.uv = np.stack([u, v], axis=1).reshape(-1, 6).astype(np.float32)
+        textures = []
+        if material == 2:
+            textures = [random_texture(16, 16, seed=seed * 31 + k, scale=4.0)]
+            m.tex = np.zeros(m.nf, dtype=np.int32)
+        d = dirs[k]
+        nrm = math.sqrt(float((d * d).sum())) or 1.0
+        pos = tuple(float(x) for x in (d / nrm * radii[k]))
+        cam = CameraData(pos, tuple(-x for x in pos), (0.0, 1.0, 0.0) if abs(d[1] / nrm) < 0.95 else (1.0, 0.0, 0.0))
+        w, h = resolutions[int(res_idx[k])]
+        flags = DEFAULT_FLAGS | (FLAT_SHADING if material == 0 else 0)
+        out.append(SceneData(f"view{k}", w, h, [ObjectData(m)], cam, textures, flags))
+    return out

@@ -137,6 +137,39 @@ int32_t gr_draw(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
 int32_t gr_draw_async(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
                       const gr_frame_params* params, uint8_t* rgba_dev, float* z_dev);
 
+/* ---- batched multi-view drawing (no counterpart in the reference, whose
+ * Draw renders one camera; each view here equals a separate gr_draw) ---- */
+typedef struct {
+  gr_frame_params params;
+  uint8_t* rgba_dev;  /* device output, width*height*4 bytes */
+  float* z_dev;       /* device output, width*height floats */
+} gr_view;
+
+/* Renders every view in one launch sequence; item i belongs to view
+ * items[i].reserved.  Asynchronous on the context stream; errors and
+ * overflow surface at gr_context_sync. */
+int32_t gr_draw_views(gr_context* ctx, const gr_view* views, int32_t num_views,
+                      const gr_draw_item* items, int32_t num_items);
+/* Binned triangles per view of the last gr_draw_views / gr_batch_run
+ * (waits for the stream). */
+int32_t gr_context_view_tpf(gr_context* ctx, int64_t* tpf, int32_t num_views);
+
+/* A fixed batch of views captured once as a CUDA graph.  With autotune != 0
+ * the raster tile size, bin slice length and persistent-grid size are chosen
+ * by timing each candidate on the batch, and the tile bins are sized to the
+ * largest bin seen.  gr_batch_run launches the graph (asynchronous);
+ * gr_batch_sync waits and, if a buffer overflowed, grows it, re-captures and
+ * re-runs the batch before returning. */
+typedef struct gr_batch gr_batch;
+int32_t gr_batch_create(gr_context* ctx, const gr_view* views, int32_t num_views,
+                        const gr_draw_item* items, int32_t num_items, int32_t autotune,
+                        gr_batch** out);
+int32_t gr_batch_run(gr_batch* batch);
+int32_t gr_batch_sync(gr_batch* batch);
+int32_t gr_batch_tuning(gr_batch* batch, int32_t* tile_size, int32_t* slice_entries,
+                        int32_t* raster_waves, int32_t* bin_capacity, float* tuned_ms);
+int32_t gr_batch_destroy(gr_batch* batch);
+
 /* ---- host math (R1: stays on the host, restated from matrix.go) ---- */
 typedef struct {
   int32_t mesh;
@@ -191,6 +224,15 @@ int32_t gr_context_flush_l2(gr_context* ctx, int64_t bytes);
  * bins overflow is re-run by gr_draw after the bins grow. */
 int32_t gr_context_set_tuning(gr_context* ctx, int32_t tile_size, int32_t bin_capacity);
 int32_t gr_context_get_tuning(gr_context* ctx, int32_t* tile_size, int32_t* bin_capacity);
+/* Raster work split: bin entries per slice (a tile whose bin is longer is
+ * shared by up to 8 CTAs) and persistent-raster waves (CTAs = SMs x resident
+ * CTAs x waves); 0 keeps the current value. */
+int32_t gr_context_set_raster(gr_context* ctx, int32_t slice_entries, int32_t raster_waves);
+/* Autotunes tile size, slice length and raster waves for this frame (the
+ * batch autotuner on a one-view batch) and sizes the bins; the choice stays
+ * on the context. */
+int32_t gr_context_autotune(gr_context* ctx, const gr_draw_item* items, int32_t num_items,
+                            const gr_frame_params* params);
 /* Number of kernels the last frame launched. */
 int32_t gr_context_last_launches(gr_context* ctx, int32_t* launches);
 /* Host<->device bytes the last gr_draw moved (draw items in; result words,
