@@ -831,6 +831,7 @@ struct RasterShape {
   static constexpr int kThreads = TS * TS / 4;  // 4 pixels per thread in the resolve
   static constexpr int kStride = TS + 8;        // padded key row: 8x4 warp blocks hit disjoint banks
   static constexpr int kWarps = kThreads / 32;
+  static constexpr int kMinBlocks = 2048 / kThreads / 2;  // 32 warps per SM: 64 registers a thread
 };
 
 // Exact depth test of one covered pixel: zRec in the reference's order,
@@ -1004,19 +1005,22 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   TriRaster* tri = s_tri[warp];
   uint32_t* trec = s_trec[warp];
   CandQueue<TS> q{s_ent[warp], tri, trec, 0};
+  // Entries per warp chunk: small bins use shorter chunks so that every warp
+  // gets some (the coverage walk below keeps all lanes busy either way).
+  const uint32_t chunk = min(32u, max(8u, (hi - lo + 2u * kWarps - 1u) / (2u * kWarps)));
   for (;;) {
-    // Phase 1: warps take 32 bin entries at a time from a shared cursor.
+    // Phase 1: warps take `chunk` bin entries at a time from a shared cursor.
     // Footprints up to kLaneArea pixels run one lane per triangle in a
     // converged loop (so covered pixels can be queued warp-synchronously);
     // larger or int64 triangles are queued for the whole CTA.
     for (;;) {
       if (*(volatile uint32_t*)&s_nlarge >= kLargeCap) break;
       uint32_t b = 0;
-      if (lane == 0) b = atomicAdd(&s_next, 32u);
+      if (lane == 0) b = atomicAdd(&s_next, chunk);
       b = __shfl_sync(FULL_MASK, b, 0);
       if (b >= hi) break;
       const uint32_t i = b + lane;
-      const bool valid = i < hi;
+      const bool valid = lane < chunk && i < hi;
       uint32_t r = 0;
       int lx0 = 0, lx1 = -1, ly0 = 0, ly1 = -1;
       TriRaster t;
@@ -1106,19 +1110,24 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     // interleaved share of their 8x4 blocks (global block index mod warps).
     int base = 0;
     for (uint32_t k = 0; k < nl; ++k) {
-      const uint32_t rr = s_large[k];
-      const TriRaster tt = a.rast[rr];
+      const uint32_t slot = 32u + (k & 31u);
+      if ((k & 31u) == 0) {
+        // slots 32..63 are about to be reused: drain, then stage the next 32
+        // large records with one load per lane
+        q.flush(skey, a, tx0, ty0);
+        if (k + lane < nl) {
+          const uint32_t r2 = s_large[k + lane];
+          tri[32 + lane] = a.rast[r2];
+          trec[32 + lane] = r2;
+        }
+        __syncwarp();
+      }
+      const TriRaster tt = tri[slot];
+      const uint32_t rr = trec[slot];
       const int bx0 = max((int)tt.bx0, tx0), bx1 = min((int)tt.bx1, tx1);
       const int by0 = max((int)tt.by0, ty0), by1 = min((int)tt.by1, ty1);
       const int nblk = ((bx1 - bx0 + 8) >> 3) * ((by1 - by0 + 4) >> 2);
       const int j0 = (warp - base + kWarps) % kWarps;
-      const uint32_t slot = 32u + (k & 31u);
-      if ((k & 31u) == 0) q.flush(skey, a, tx0, ty0);  // slots 32..63 are about to be reused
-      if (lane == 0) {
-        tri[slot] = tt;
-        trec[slot] = rr;
-      }
-      __syncwarp();
       walk_blocks<TS>(q, skey, a, tt, rr, slot, bx0, bx1, by0, by1, j0, kWarps, tx0, ty0);
       base = (base + nblk) % kWarps;
     }
@@ -1260,7 +1269,7 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
 // Persistent raster: CTAs take work items from the queue until it is empty;
 // the last CTA to finish publishes and resets the frame's counters.
 template <int TS>
-__global__ void __launch_bounds__(RasterShape<TS>::kThreads) k_raster(const FrameArgs a) {
+__global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kMinBlocks) k_raster(const FrameArgs a) {
   __shared__ RasterSmem<TS> sm;
   __shared__ uint32_t s_item, s_tile, s_slice, s_lastcta;
   __shared__ int s_view;
