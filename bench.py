@@ -147,6 +147,10 @@ def run_ours(args):
     L = N.lib()
     # device outputs owned by the context (NULL pointers)
     n = len(scene.objects)
+    # tile size, raster slice and bin capacity for this frame, picked by the
+    # library's autotuner (part of warm-up)
+    N.check(L.gr_context_autotune(ctx.handle, up.items, n, C.byref(up.params)))
+    tuning = ctx.tuning()
     for _ in range(max(3, args.warmup)):
         gr.draw_async(ctx, up.items, n, up.params)
         ctx.flush_l2()
@@ -193,6 +197,8 @@ def run_ours(args):
         kms += np.array(buf[:])
         ctx.flush_l2()
     kms /= kprof
+    # the profiled pass brackets three phases: k_light + k_project | k_clip +
+    # k_bin_big | k_plan + k_raster (k_plan is a one-thread-per-tile scan)
     names = ["k_project", "k_bin_big", "k_raster"]
     top = int(np.argmax(kms))
     ab = algorithmic_bytes(scene)
@@ -226,6 +232,9 @@ def run_ours(args):
     N.check(L.gr_host_free(hp))
     e2e_value = faces * e2e_frames * ws / e2e_s / 1e6
 
+    batched = bench_batched(ctx, args, local) if not args.skip_batched else None
+    stress = bench_stress(ctx, args) if not args.skip_batched else None
+
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
@@ -239,7 +248,8 @@ def run_ours(args):
         "data": "synthetic (seeded heightfield, seeded 16x16 RGBA8 texture)",
         "config": {"workload": WORKLOAD, "faces": faces, "width": W, "height": H,
                    "binned_triangles": int(tpf.value), "parallelism": f"replicas x{ws}",
-                   "l2": "flushed between frames (512 MiB write outside the timed events)"},
+                   "l2": "flushed between frames (512 MiB write outside the timed events)",
+                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_entries": ctx.raster()[0]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
                 "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
@@ -251,6 +261,8 @@ def run_ours(args):
                      "frame_algorithmic_bytes": int(ab["frame"])},
         "gpu_launches": int(launches_per_frame * args.steps),
         "clocks": sampler.summary(),
+        "batched_multiview": batched,
+        "stress_1080p": stress,
     }
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(scene, args)
@@ -258,6 +270,112 @@ def run_ours(args):
     ctx.close()
     if pg:
         pg.destroy_process_group()
+
+
+def bench_batched(ctx, args, device):
+    """256 seeded views (heightfields and icospheres, 100..200k triangles
+    log-uniform, four resolutions, mixed materials): one autotuned CUDA-graph
+    batch against the same views drawn by plain per-view launches
+    (gr_draw_async, one per view, back to back on the same stream).  Both are
+    device-timed with events on the library stream; outputs (820 MB) exceed
+    L2, so no flush is needed.  The two outputs are compared bit for bit."""
+    import torch
+    from gorender_gb300 import renderer as R
+    from gorender_gb300 import scenes
+
+    vs = scenes.multiview_batch(256, seed=0)
+    dev = torch.device("cuda", device)
+    views, entries, plain = [], [], []
+    for v, sc in enumerate(vs):
+        up = R.UploadedScene(ctx, sc)
+        bufs = [torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device=dev),
+                torch.empty((sc.height, sc.width), dtype=torch.float32, device=dev),
+                torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device=dev),
+                torch.empty((sc.height, sc.width), dtype=torch.float32, device=dev)]
+        views.append((up.params, bufs[0].data_ptr(), bufs[1].data_ptr()))
+        for h, (mvp, w) in zip(up.mesh_handles, up.matrices):
+            entries.append((h, mvp, w, v))
+        plain.append((up, bufs))
+    torch.cuda.synchronize(dev)
+    faces = sum(sc.num_triangles for sc in vs)
+    pixels = sum(sc.width * sc.height for sc in vs)
+    b = R.Batch(ctx, views, entries, autotune=True)
+    tuning = b.tuning()
+    reps = 10
+    for _ in range(3):
+        b.run()
+    b.sync()
+    ctx.sync()
+    t_batch = []
+    for _ in range(reps):
+        ctx.event(0)
+        b.run()
+        ctx.event(1)
+        b.sync()
+        t_batch.append(ctx.elapsed_ms(0, 1))
+
+    def plain_pass():
+        for up, bufs in plain:
+            R.draw_async(ctx, up.items, len(up.scene.objects), up.params, bufs[2].data_ptr(), bufs[3].data_ptr())
+
+    for _ in range(2):
+        plain_pass()
+        try:
+            ctx.sync()
+        except R.N.GrError as e:  # the first pass may grow the bins; it is re-issued
+            if e.code != R.N.GR_ERR_BIN_OVERFLOW:
+                raise
+    t_plain = []
+    for _ in range(reps):
+        ctx.event(2)
+        plain_pass()
+        ctx.event(3)
+        ctx.sync()
+        t_plain.append(ctx.elapsed_ms(2, 3))
+    b.run()
+    b.sync()
+    same = all(torch.equal(bufs[0], bufs[2]) and torch.equal(bufs[1].view(torch.int32), bufs[3].view(torch.int32))
+               for _, bufs in plain)
+    launches = ctx.last_launches()
+    mb, mp = statistics.median(t_batch), statistics.median(t_plain)
+    b.close()
+    return {"views": len(vs), "faces": faces, "pixels": pixels,
+            "graph_ms": round(mb, 4), "plain_ms": round(mp, 4),
+            "views_per_s": round(len(vs) / (mb * 1e-3), 1), "plain_views_per_s": round(len(vs) / (mp * 1e-3), 1),
+            "Mtris_per_s": round(faces / (mb * 1e-3) / 1e6, 2),
+            "plain_Mtris_per_s": round(faces / (mp * 1e-3) / 1e6, 2),
+            "speedup_vs_plain": round(mp / mb, 3), "identical_output": bool(same), "reps": reps,
+            "tuning": tuning, "kernel_launches_per_batch": launches}
+
+
+def bench_stress(ctx, args):
+    """The 64-icosphere 1920x1080 scene (3.6M faces, per-vertex colours):
+    device-timed frames after the autotuner, L2 flushed between frames."""
+    import ctypes as C
+    from gorender_gb300 import _native as N
+    from gorender_gb300 import renderer as R
+    from gorender_gb300 import scenes
+
+    sc = scenes.scene_icospheres_1920x1080()
+    up = R.UploadedScene(ctx, sc)
+    n = len(sc.objects)
+    N.check(N.lib().gr_context_autotune(ctx.handle, up.items, n, C.byref(up.params)))
+    for _ in range(3):
+        R.draw_async(ctx, up.items, n, up.params)
+    ctx.sync()
+    frames = 30
+    t = []
+    for _ in range(frames):
+        ctx.event(4)
+        R.draw_async(ctx, up.items, n, up.params)
+        ctx.event(5)
+        ctx.flush_l2()
+        ctx.sync()
+        t.append(ctx.elapsed_ms(4, 5))
+    ms = statistics.median(t)
+    return {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
+            "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
+            "frames": frames, "tile_size": ctx.tuning()[0], "slice_entries": ctx.raster()[0]}
 
 
 def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):
@@ -336,6 +454,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-batched", action="store_true", help="only the plain heightfield frame")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

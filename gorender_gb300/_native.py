@@ -35,7 +35,8 @@ EXPORTS = [
     "gr_context_last_launches", "gr_context_last_transfer_bytes", "gr_draw_profiled", "gr_host_alloc",
     "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning", "gr_draw_noalloc",
     "gr_draw_views", "gr_context_view_tpf", "gr_batch_create", "gr_batch_run", "gr_batch_sync",
-    "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_autotune",
+    "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_get_raster",
+    "gr_context_autotune",
 ]
 
 
@@ -145,6 +146,7 @@ def lib() -> C.CDLL:
             "gr_batch_tuning": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), fp],
             "gr_batch_destroy": [vp],
             "gr_context_set_raster": [vp, i32, i32],
+            "gr_context_get_raster": [vp, C.POINTER(i32), C.POINTER(i32)],
             "gr_context_autotune": [vp, C.POINTER(DrawItem), i32, C.POINTER(FrameParams)],
         }
         for name, args in sig.items():

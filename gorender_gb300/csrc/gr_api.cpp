@@ -73,8 +73,13 @@ struct gr_context {
   bool texs_dirty = true;
 
   DevItem* d_items = nullptr;
-  DevItem* h_items = nullptr;  // pinned staging
+  DevItem* h_items = nullptr;  // pinned staging: kStageSlots slots of items_cap items
   int items_cap = 0;
+  // Pinned staging ring: back-to-back asynchronous draws write the next slot;
+  // a slot is rewritten only after the copies that read it have run.
+  cudaEvent_t stage_ev[kStageSlots] = {};
+  bool stage_used[kStageSlots] = {};
+  int stage_slot = 0;
 
   TriRaster* rast = nullptr;
   TriShade* shade = nullptr;
@@ -97,7 +102,7 @@ struct gr_context {
   float* vlight = nullptr;          // per-normal Gouraud intensities
   uint64_t vlight_cap = 0;
   DevView* d_views = nullptr;       // view table (device) and its pinned staging
-  DevView* h_views = nullptr;
+  DevView* h_views = nullptr;       // kStageSlots slots of views_cap views
   unsigned long long* view_tpf = nullptr;
   unsigned long long* view_tpf_out = nullptr;
   unsigned long long* h_view_tpf = nullptr;
@@ -183,7 +188,7 @@ int32_t ensure_items(gr_context* c, int n) {
   c->items_cap = 0;
   int32_t st = dev_alloc(&c->d_items, cap);
   if (st) return st;
-  CK(cudaMallocHost((void**)&c->h_items, sizeof(DevItem) * cap));
+  CK(cudaMallocHost((void**)&c->h_items, sizeof(DevItem) * cap * kStageSlots));
   c->items_cap = cap;
   return GR_OK;
 }
@@ -318,7 +323,7 @@ int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
         (st = dev_alloc(&c->view_tpf_out, cap)))
       return st;
     CK(cudaMemsetAsync(c->view_tpf, 0, sizeof(unsigned long long) * cap, c->stream));
-    CK(cudaMallocHost((void**)&c->h_views, sizeof(DevView) * cap));
+    CK(cudaMallocHost((void**)&c->h_views, sizeof(DevView) * cap * kStageSlots));
     CK(cudaMallocHost((void**)&c->h_view_tpf, sizeof(unsigned long long) * cap));
     c->views_cap = cap;
   }
@@ -361,10 +366,14 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   if (st) return st;
   if ((st = upload_textures(c))) return st;
   if ((st = ensure_views(c, nviews, total_tiles))) return st;
+  const int slot = (c->stage_slot + 1) % kStageSlots;
+  if (c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
+  DevView* hviews = c->h_views + (size_t)slot * c->views_cap;
+  DevItem* hitems = c->h_items + (size_t)slot * c->items_cap;
   uint32_t tile_base = 0;
   for (int v = 0; v < nviews; ++v) {
     const gr_frame_params* p = views[v].p;
-    DevView& d = c->h_views[v];
+    DevView& d = hviews[v];
     std::memset(&d, 0, sizeof(d));
     d.W = p->width;
     d.H = p->height;
@@ -398,7 +407,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     const uint64_t fb = faces;
     faces += (uint64_t)mr.nf;
     if (mr.nf == 0) continue;  // an empty mesh draws nothing
-    DevItem& d = c->h_items[live++];
+    DevItem& d = hitems[live++];
     std::memcpy(d.mvp, items[i].mvp, sizeof(d.mvp));
     std::memcpy(d.world, items[i].world, sizeof(d.world));
     std::memcpy(d.bbox, mr.bbox, sizeof(d.bbox));
@@ -430,8 +439,11 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // a graph batch keeps its own tables, so other draws cannot overwrite them
   DevView* dviews = own_views ? own_views : c->d_views;
   DevItem* ditems = own_items ? own_items : c->d_items;
-  CK(cudaMemcpyAsync(dviews, c->h_views, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
-  if (live) CK(cudaMemcpyAsync(ditems, c->h_items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(dviews, hviews, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
+  if (live) CK(cudaMemcpyAsync(ditems, hitems, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaEventRecord(c->stage_ev[slot], c->stream));
+  c->stage_used[slot] = true;
+  c->stage_slot = slot;
   c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
   c->d2h_bytes = 0;
 
@@ -596,6 +608,8 @@ int32_t gr_context_create(int32_t device, gr_context** out) {
   if (e == cudaSuccess) e = cudaMemset(c->d_result, 0, sizeof(DevResult));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_result, sizeof(DevResult));
   for (int i = 0; i < 64 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->events[i]);
+  for (int i = 0; i < kStageSlots && e == cudaSuccess; ++i)
+    e = cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gr_context_destroy(c);
     return fail(GR_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
@@ -626,6 +640,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->fb_rgba); dev_free(c->fb_z);
   if (c->flush_buf) cudaFree(c->flush_buf);
   for (auto& ev : c->events) if (ev) cudaEventDestroy(ev);
+  for (auto& ev : c->stage_ev) if (ev) cudaEventDestroy(ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GR_OK;
@@ -939,7 +954,8 @@ int32_t batch_autotune(gr_batch* b) {
   struct Cfg {
     int shift, slice, waves;
   };
-  const Cfg cands[] = {{5, 128, 1}, {5, 64, 1}, {5, 256, 1}, {5, 128, 2}, {4, 128, 1}, {4, 64, 1}, {4, 256, 1}, {4, 128, 2}};
+  // tile size (and with it the raster CTA: TS*TS/4 threads) x bin entries per raster slice
+  const Cfg cands[] = {{5, 128, 1}, {5, 64, 1}, {5, 256, 1}, {4, 32, 1}, {4, 64, 1}, {4, 128, 1}, {4, 256, 1}};
   Cfg best = cands[0];
   float best_ms = 1e30f;
   for (const Cfg& k : cands) {
@@ -1265,6 +1281,13 @@ int32_t gr_context_set_raster(gr_context* c, int32_t slice_entries, int32_t rast
   std::lock_guard<std::mutex> lk(c->mu);
   if (slice_entries) c->slice_entries = (uint32_t)slice_entries;
   if (raster_waves) c->raster_waves = raster_waves;
+  return GR_OK;
+}
+
+int32_t gr_context_get_raster(gr_context* c, int32_t* slice_entries, int32_t* raster_waves) {
+  if (!c || !slice_entries || !raster_waves) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *slice_entries = (int32_t)c->slice_entries;
+  *raster_waves = c->raster_waves;
   return GR_OK;
 }
 

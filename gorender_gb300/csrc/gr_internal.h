@@ -16,6 +16,7 @@ constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes 
 constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
 constexpr int kProjectThreads = 256;
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
+constexpr int kStageSlots = 3;                // pinned staging slots for back-to-back async draws
 constexpr int kRasterMaxSlices = 32;          // CTAs that may share one tile's bin
 constexpr int kDefaultSliceEntries = 128;     // bin entries per slice before a tile is split
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)

@@ -112,7 +112,7 @@ class Context:
         return self._h
 
     def close(self):
-        for b in self._batches:
+        for b in list(self._batches):
             b.close()
         self._batches = []
         if self._h:
@@ -189,6 +189,12 @@ class Context:
         t, b = C.c_int32(), C.c_int32()
         N.check(N.lib().gr_context_get_tuning(self._h, C.byref(t), C.byref(b)))
         return int(t.value), int(b.value)
+
+    def raster(self) -> Tuple[int, int]:
+        """(bin entries per raster slice, persistent-raster waves)."""
+        s, w = C.c_int32(), C.c_int32()
+        N.check(N.lib().gr_context_get_raster(self._h, C.byref(s), C.byref(w)))
+        return int(s.value), int(w.value)
 
     def last_launches(self) -> int:
         n = C.c_int32()
@@ -416,6 +422,8 @@ class Batch:
         if self._h:
             N.lib().gr_batch_destroy(self._h)
             self._h = C.c_void_p()
+        if self in self.ctx._batches:
+            self.ctx._batches.remove(self)
 
     def __del__(self):
         try:

@@ -225,9 +225,10 @@ int32_t gr_context_flush_l2(gr_context* ctx, int64_t bytes);
 int32_t gr_context_set_tuning(gr_context* ctx, int32_t tile_size, int32_t bin_capacity);
 int32_t gr_context_get_tuning(gr_context* ctx, int32_t* tile_size, int32_t* bin_capacity);
 /* Raster work split: bin entries per slice (a tile whose bin is longer is
- * shared by up to 8 CTAs) and persistent-raster waves (CTAs = SMs x resident
+ * shared by up to 32 CTAs) and persistent-raster waves (CTAs = SMs x resident
  * CTAs x waves); 0 keeps the current value. */
 int32_t gr_context_set_raster(gr_context* ctx, int32_t slice_entries, int32_t raster_waves);
+int32_t gr_context_get_raster(gr_context* ctx, int32_t* slice_entries, int32_t* raster_waves);
 /* Autotunes tile size, slice length and raster waves for this frame (the
  * batch autotuner on a one-view batch) and sizes the bins; the choice stays
  * on the context. */

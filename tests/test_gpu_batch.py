@@ -97,3 +97,34 @@ def test_batch_view_index_checked():
             R.draw_views(ctx, [(p, r, z) for p, r, z, _, _ in views], bad)
     finally:
         ctx.close()
+
+
+def test_back_to_back_async_draws_keep_their_own_tables():
+    """Plain asynchronous draws of different views issued without a sync in
+    between: each must render its own items (the pinned staging of one draw is
+    not overwritten by the next before its copy has run)."""
+    ctx = gr.Context(0)
+    try:
+        views, entries, singles = _setup(ctx, _small_views(9, seed=11))
+        per_view = [[] for _ in views]
+        for m, mvp, w, v in entries:
+            per_view[v].append((m, mvp, w))
+        items = [R.make_items(e) for e in per_view]
+        for _ in range(2):  # the first pass may grow buffers (reported at sync)
+            for _, _, _, rgba, z in views:
+                rgba.zero_()
+                z.zero_()
+            torch.cuda.synchronize()
+            for v, (params, rp, zp, _, _) in enumerate(views):
+                R.draw_async(ctx, items[v], len(per_view[v]), params, rp, zp)
+            try:
+                ctx.sync()
+                break
+            except gr.GrError as e:
+                assert e.code == R.N.GR_ERR_BIN_OVERFLOW
+        for v, (params, _, _, rgba, z) in enumerate(views):
+            ref_rgba, ref_z, _ = singles[v].render()
+            assert np.array_equal(rgba.cpu().numpy(), ref_rgba), f"view {v}: RGBA differs"
+            assert np.array_equal(z.cpu().numpy().view(np.uint32), ref_z.view(np.uint32)), f"view {v}: Z differs"
+    finally:
+        ctx.close()
