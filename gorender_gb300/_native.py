@@ -36,7 +36,8 @@ EXPORTS = [
     "gr_host_free", "gr_context_set_tuning", "gr_context_get_tuning", "gr_draw_noalloc",
     "gr_draw_views", "gr_context_view_tpf", "gr_batch_create", "gr_batch_run", "gr_batch_sync",
     "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_get_raster",
-    "gr_context_autotune",
+    "gr_context_autotune", "gr_diff_create", "gr_diff_forward", "gr_diff_backward", "gr_diff_buffers",
+    "gr_diff_destroy",
 ]
 
 
@@ -76,6 +77,22 @@ class Camera(C.Structure):
 class View(C.Structure):
     """gr_view: one view of a batch."""
     _fields_ = [("params", FrameParams), ("rgba_dev", C.c_void_p), ("z_dev", C.c_void_p)]
+
+
+class DiffView(C.Structure):
+    """gr_diff_view: one view of the differentiable object."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("flags", C.c_uint32), ("reserved", C.c_int32),
+                ("screen", C.c_float * 16), ("mvp", C.c_float * 16)]
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("vertex_colors", C.c_void_p), ("texture", C.c_void_p),
+                ("light", C.c_float * 3), ("reserved", C.c_int32)]
+
+
+class DiffGrads(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("vertex_colors", C.c_void_p), ("texture", C.c_void_p),
+                ("light", C.c_double * 3)]
 
 
 class NoallocObject(C.Structure):
@@ -148,6 +165,11 @@ def lib() -> C.CDLL:
             "gr_context_set_raster": [vp, i32, i32],
             "gr_context_get_raster": [vp, C.POINTER(i32), C.POINTER(i32)],
             "gr_context_autotune": [vp, C.POINTER(DrawItem), i32, C.POINTER(FrameParams)],
+            "gr_diff_create": [vp, i32, fp, i32, i32, C.POINTER(DiffView), i32, C.POINTER(vp)],
+            "gr_diff_forward": [vp, C.POINTER(DiffParams), vp, vp, C.POINTER(C.c_double)],
+            "gr_diff_backward": [vp, C.POINTER(DiffGrads)],
+            "gr_diff_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int64)],
+            "gr_diff_destroy": [vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)

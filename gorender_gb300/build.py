@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgorender_cuda.so")
 
-SOURCES = ["gr_kernels.cu", "gr_api.cpp", "gr_host_math.cpp", "gr_noalloc.cu"]
+SOURCES = ["gr_kernels.cu", "gr_api.cpp", "gr_host_math.cpp", "gr_noalloc.cu", "gr_diff.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math,-Wall",

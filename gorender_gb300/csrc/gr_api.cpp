@@ -1325,4 +1325,276 @@ int32_t gr_context_last_launches(gr_context* c, int32_t* launches) {
   return GR_OK;
 }
 
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiable forward/backward (an extension; see the header)
+// ---------------------------------------------------------------------------
+struct gr_diff {
+  gr_context* ctx = nullptr;
+  int mesh = -1;
+  int nv = 0, nf = 0, nn = 0;
+  int tw = 0, th = 0;
+  std::vector<gr_frame_params> params;  // per view: visibility flags + screen matrix
+  std::vector<ViewIn> vin;
+  std::vector<gr_draw_item> items;      // one item per view
+  std::vector<DiffView> hviews;
+  uint64_t pixels = 0;
+  int max_pixels = 0;
+  DiffView* d_views = nullptr;
+  DevView* d_frame_views = nullptr;     // the visibility pass's own tables
+  DevItem* d_items = nullptr;
+  uint32_t* ids = nullptr;              // per pixel: visible face
+  float* z = nullptr;                   // per pixel: zRec of the visible face
+  DiffRecord* rec = nullptr;
+  float* nhat = nullptr;
+  float* d_world = nullptr;
+  double* d_acc = nullptr;              // loss, light gradient x 3
+  double* h_acc = nullptr;              // pinned
+  gr_diff_params last{};                // parameters of the last forward
+  const float* last_target = nullptr;
+  bool have_forward = false;
+};
+
+namespace {
+
+DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* target) {
+  DiffArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const MeshRec& mr = d->ctx->meshes[d->mesh];
+  a.views = d->d_views;
+  a.num_views = (int)d->hviews.size();
+  a.max_pixels = d->max_pixels;
+  a.nv = d->nv; a.nf = d->nf; a.nn = d->nn;
+  a.pos = p.positions;
+  a.vcol = p.vertex_colors;
+  a.tex = p.texture;
+  a.tw = d->tw; a.th = d->th;
+  for (int k = 0; k < 3; ++k) a.L[k] = p.light[k];
+  a.vidx = mr.vidx;
+  a.nidx = mr.nidx;
+  a.uv = mr.uv;
+  a.nhat = d->nhat;
+  a.ids = d->ids;
+  a.rec = d->rec;
+  a.target = target;
+  a.loss = d->d_acc;
+  a.g_light = d->d_acc + 1;
+  return a;
+}
+
+void diff_free(gr_diff* d) {
+  dev_free(d->d_views); dev_free(d->d_frame_views); dev_free(d->d_items);
+  dev_free(d->ids); dev_free(d->z); dev_free(d->rec); dev_free(d->nhat); dev_free(d->d_world);
+  dev_free(d->d_acc);
+  if (d->h_acc) cudaFreeHost(d->h_acc);
+  d->h_acc = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t texture_width,
+                       int32_t texture_height, const gr_diff_view* views, int32_t num_views, gr_diff** out) {
+  if (!c || !world || !views || !out || num_views <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  if (mesh < 0 || mesh >= (int)c->meshes.size() || !c->meshes[mesh].alive)
+    return fail(GR_ERR_INVALID_ARGUMENT, "unknown mesh %d", mesh);
+  const MeshRec& mr = c->meshes[mesh];
+  if (mr.nn <= 0 || !mr.has_nidx || !mr.nidx_ok)
+    return fail(GR_ERR_INVALID_ARGUMENT, "the differentiable mesh needs vertex normals with valid normal indices");
+  if (mr.nf <= 0 || mr.nv <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "empty mesh");
+  if (texture_width < 0 || texture_height < 0 || (texture_width == 0) != (texture_height == 0))
+    return fail(GR_ERR_INVALID_ARGUMENT, "bad texture size %dx%d", texture_width, texture_height);
+  if ((uint64_t)mr.nf * (uint64_t)num_views >= (1ull << 28))
+    return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces over all views");
+  gr_diff* d = new (std::nothrow) gr_diff();
+  if (!d) return fail(GR_ERR_OUT_OF_MEMORY, "diff allocation");
+  d->ctx = c;
+  d->mesh = mesh;
+  d->nv = mr.nv; d->nf = mr.nf; d->nn = mr.nn;
+  d->tw = texture_width; d->th = texture_height;
+  d->params.resize(num_views);
+  d->items.resize(num_views);
+  d->hviews.resize(num_views);
+  uint64_t pix = 0;
+  int32_t st = GR_OK;
+  for (int v = 0; v < num_views && !st; ++v) {
+    const gr_diff_view& dv = views[v];
+    if (dv.width <= 0 || dv.height <= 0 || dv.width > kMaxDim || dv.height > kMaxDim) {
+      st = fail(GR_ERR_INVALID_ARGUMENT, "view %d: bad size %dx%d", v, dv.width, dv.height);
+      break;
+    }
+    gr_frame_params& p = d->params[v];
+    std::memset(&p, 0, sizeof(p));
+    p.width = dv.width;
+    p.height = dv.height;
+    p.flags = (dv.flags & (GR_FRUSTUM_CLIPPING | GR_BACKFACE_CULLING)) | GR_SHOW_FACES | kViewFaceIds;
+    std::memcpy(p.screen, dv.screen, sizeof(p.screen));
+    gr_draw_item& it = d->items[v];
+    it.mesh = mesh;
+    it.reserved = v;
+    std::memcpy(it.mvp, dv.mvp, sizeof(it.mvp));
+    std::memcpy(it.world, world, sizeof(it.world));
+    DiffView& hv = d->hviews[v];
+    hv.W = dv.width;
+    hv.H = dv.height;
+    hv.pix_base = (uint32_t)pix;
+    hv.face_base = (uint32_t)((uint64_t)v * (uint64_t)mr.nf);
+    // Q = rows 0 and 1 of S * MVP (homogeneous screen x and y) and row 3 of
+    // MVP (clip W), in double: products of two floats are exact there
+    for (int j = 0; j < 4; ++j) {
+      double q0 = 0.0, q1 = 0.0;
+      for (int i = 0; i < 4; ++i) {
+        q0 += (double)dv.screen[i] * (double)dv.mvp[4 * i + j];
+        q1 += (double)dv.screen[4 + i] * (double)dv.mvp[4 * i + j];
+      }
+      hv.Q[j] = q0;
+      hv.Q[4 + j] = q1;
+      hv.Q[8 + j] = (double)dv.mvp[12 + j];
+    }
+    pix += (uint64_t)dv.width * (uint64_t)dv.height;
+    d->max_pixels = std::max(d->max_pixels, dv.width * dv.height);
+    if (pix >= (1ull << 32)) st = fail(GR_ERR_UNSUPPORTED, "more than 2^32 pixels over all views");
+  }
+  d->pixels = pix;
+  if (!st) st = dev_alloc(&d->d_views, (size_t)num_views);
+  if (!st) st = dev_alloc(&d->d_frame_views, (size_t)num_views);
+  if (!st) st = dev_alloc(&d->d_items, (size_t)num_views);
+  if (!st) st = dev_alloc(&d->ids, (size_t)pix);
+  if (!st) st = dev_alloc(&d->z, (size_t)pix);
+  if (!st) st = dev_alloc(&d->rec, (size_t)pix);
+  if (!st) st = dev_alloc(&d->nhat, (size_t)mr.nn * 4);
+  if (!st) st = dev_alloc(&d->d_world, (size_t)16);
+  if (!st) st = dev_alloc(&d->d_acc, (size_t)4);
+  if (!st && cudaMallocHost((void**)&d->h_acc, 4 * sizeof(double)) != cudaSuccess) {
+    d->h_acc = nullptr;
+    st = fail(GR_ERR_OUT_OF_MEMORY, "pinned accumulator");
+  }
+  if (!st) {
+    d->vin.resize(num_views);
+    for (int v = 0; v < num_views; ++v)
+      d->vin[v] = ViewIn{&d->params[v], d->ids + d->hviews[v].pix_base, d->z + d->hviews[v].pix_base};
+    cudaError_t e = cudaMemcpyAsync(d->d_views, d->hviews.data(), sizeof(DiffView) * num_views,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d->d_world, world, 16 * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) st = fail(GR_ERR_CUDA, "diff tables: %s", cudaGetErrorString(e));
+  }
+  if (!st) {
+    int e = launch_diff_normals(d->d_world, mr.vnrm, mr.nn, d->nhat, c->stream);
+    if (!e) e = (int)cudaStreamSynchronize(c->stream);
+    if (e) st = fail(GR_ERR_CUDA, "diff normals: %s", cudaGetErrorString((cudaError_t)e));
+  }
+  if (st) {
+    cudaStreamSynchronize(c->stream);
+    diff_free(d);
+    delete d;
+    return st;
+  }
+  *out = d;
+  return GR_OK;
+}
+
+int32_t gr_diff_forward(gr_diff* d, const gr_diff_params* p, const float* target_dev, float* image_dev,
+                        double* loss) {
+  if (!d || !p || !target_dev) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->positions || !p->vertex_colors) return fail(GR_ERR_INVALID_ARGUMENT, "positions and colours are required");
+  if (!is_device_ptr(p->positions) || !is_device_ptr(p->vertex_colors) || !is_device_ptr(target_dev) ||
+      (p->texture && !is_device_ptr(p->texture)) || (image_dev && !is_device_ptr(image_dev)))
+    return fail(GR_ERR_INVALID_ARGUMENT, "parameters, target and image must be device pointers");
+  if ((uintptr_t)p->positions % 16 || (uintptr_t)target_dev % 16 || (p->texture && (uintptr_t)p->texture % 16) ||
+      (image_dev && (uintptr_t)image_dev % 16))
+    return fail(GR_ERR_INVALID_ARGUMENT, "positions, texture, target and image need 16-byte alignment");
+  if (p->texture && d->tw == 0) return fail(GR_ERR_INVALID_ARGUMENT, "created without a texture size");
+  gr_context* c = d->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  MeshRec& mr = c->meshes[d->mesh];
+  if (!mr.alive) return fail(GR_ERR_INVALID_ARGUMENT, "the mesh was destroyed");
+  const int nviews = (int)d->params.size();
+  DiffArgs a = diff_args(d, *p, target_dev);
+  a.image = image_dev;
+  for (int attempt = 0; attempt < 5; ++attempt) {
+    // visibility with the parameter positions: the item tables take the
+    // mesh's pointers, so the mesh briefly points at them
+    float* keep = mr.pos;
+    mr.pos = const_cast<float*>(p->positions);
+    Prepared pr;
+    int32_t st = prepare(c, d->vin.data(), nviews, d->items.data(), nviews, true, pr, d->d_frame_views,
+                         d->d_items);
+    mr.pos = keep;
+    if (st) return st;
+    int e = launch_diff_bbox(p->positions, d->nv, d->d_items, nviews, c->stream);
+    if (e) return fail(GR_ERR_CUDA, "diff bbox: %s", cudaGetErrorString((cudaError_t)e));
+    if ((st = launch(c, pr.a))) return st;
+    CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(d->d_acc, 0, sizeof(double), c->stream));
+    e = launch_diff_forward(a, c->stream);
+    if (e) return fail(GR_ERR_CUDA, "diff forward: %s", cudaGetErrorString((cudaError_t)e));
+    CK(cudaMemcpyAsync(d->h_acc, d->d_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int32_t err;
+    const int rerun = check_result(c, *c->h_result, &err);
+    if (err) return err;
+    if (rerun) continue;
+    d->last = *p;
+    d->last_target = target_dev;
+    d->have_forward = true;
+    if (loss) *loss = d->h_acc[0];
+    return GR_OK;
+  }
+  return fail(GR_ERR_OUT_OF_MEMORY, "frame buffers kept overflowing after resizing");
+}
+
+int32_t gr_diff_backward(gr_diff* d, gr_diff_grads* g) {
+  if (!d || !g) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!d->have_forward) return fail(GR_ERR_INVALID_ARGUMENT, "gr_diff_backward before gr_diff_forward");
+  if (!g->positions || !g->vertex_colors || !is_device_ptr(g->positions) || !is_device_ptr(g->vertex_colors) ||
+      (g->texture && !is_device_ptr(g->texture)))
+    return fail(GR_ERR_INVALID_ARGUMENT, "gradient buffers must be device pointers");
+  if (d->last.texture && !g->texture) return fail(GR_ERR_INVALID_ARGUMENT, "texture gradient buffer is NULL");
+  gr_context* c = d->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  DiffArgs a = diff_args(d, d->last, d->last_target);
+  a.g_pos = g->positions;
+  a.g_vcol = g->vertex_colors;
+  a.g_tex = d->last.texture ? g->texture : nullptr;
+  CK(cudaMemsetAsync(g->positions, 0, sizeof(float) * 4 * (size_t)d->nv, c->stream));
+  CK(cudaMemsetAsync(g->vertex_colors, 0, sizeof(float) * 3 * (size_t)d->nv, c->stream));
+  if (a.g_tex) CK(cudaMemsetAsync(a.g_tex, 0, sizeof(float) * 4 * (size_t)d->tw * (size_t)d->th, c->stream));
+  CK(cudaMemsetAsync(d->d_acc + 1, 0, 3 * sizeof(double), c->stream));
+  int e = launch_diff_backward(a, c->stream);
+  if (e) return fail(GR_ERR_CUDA, "diff backward: %s", cudaGetErrorString((cudaError_t)e));
+  CK(cudaMemcpyAsync(d->h_acc + 1, d->d_acc + 1, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 3; ++k) g->light[k] = d->h_acc[1 + k];
+  return GR_OK;
+}
+
+int32_t gr_diff_buffers(gr_diff* d, const uint32_t** face_ids, const void** records, int64_t* pixels) {
+  if (!d) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (face_ids) *face_ids = d->ids;
+  if (records) *records = d->rec;
+  if (pixels) *pixels = (int64_t)d->pixels;
+  return GR_OK;
+}
+
+int32_t gr_diff_destroy(gr_diff* d) {
+  if (!d) return GR_OK;
+  {
+    std::lock_guard<std::mutex> lk(d->ctx->mu);
+    cudaSetDevice(d->ctx->device);
+    cudaStreamSynchronize(d->ctx->stream);
+    diff_free(d);
+  }
+  delete d;
+  return GR_OK;
+}
+
 }  // extern "C"

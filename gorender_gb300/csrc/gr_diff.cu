@@ -1,0 +1,397 @@
+// gr_diff.cu -- differentiable shading on top of the exact visibility pass.
+//
+// This is an extension with no counterpart in the reference renderer.  The
+// frame pipeline (gr_kernels.cu) resolves visibility exactly as
+// FrameBuffer.Triangle does (rasterizer.go:90-183) and, for views flagged
+// kViewFaceIds, writes the winning face per pixel instead of a colour.  The
+// kernels here add a smooth shading model over that fixed visibility:
+//
+//   screen position of corner i   s_i = S * (clip_i / W_i)          clip_i = MVP * p_i
+//   edge functions at pixel (x,y) e_0 = (x1-x)(y2-y) - (x2-x)(y1-y)  (and cyclic)
+//   perspective barycentrics      b_i = (e_i / W_i) / sum_j (e_j / W_j)
+//   clipped to the triangle       l_i = max(b_i, 0) / sum_j max(b_j, 0)
+//
+// The barycentrics are evaluated in the 2D homogeneous form (Olano and Greer,
+// "Triangle scan conversion using 2D homogeneous coordinates", 1997), which
+// needs no perspective divide: with Q = S * MVP,
+//   u_i = (Q_0 - x Q_3) . p_i,  v_i = (Q_1 - y Q_3) . p_i       (= (s_i - pixel) * W_i)
+//   D_0 = u_1 v_2 - u_2 v_1 (and cyclic),  b_i = D_i / (D_0 + D_1 + D_2)
+// in double precision: u and v cancel screen positions of hundreds of pixels
+// down to a few, and on thin faces b amplifies what is left, so float32 leaves
+// relative errors up to ~1e-3 where double leaves ~1e-12.
+//   colour                        c   = sum_i l_i c_i               (vertex RGB)
+//   intensity                     I   = sum_i l_i (0.5 + 0.5 nhat_i . L)
+//   texel                         t   = tex[floor(v th) mod th][floor(u tw) mod tw],  (u,v) = sum_i l_i uv_i
+//   pixel                         out = (I c_r t_r, I c_g t_g, I c_b t_b, t_a)
+//   loss                          sum over pixels and channels of (out - target)^2
+//
+// nhat_i is the renderer's Gouraud normal, xyz of Vec4.Normalize(world * n)
+// (renderer.go:328-331); vertex normals are fixed inputs.  The forward pass
+// stores per pixel the face, the texel and (l0, l1); the backward pass reads
+// them back, recomputes the shading and accumulates the gradients of the loss
+// with respect to vertex colours, texels, the light direction and vertex
+// positions.  Position gradients flow through the barycentrics only (the
+// interior term): visibility and texel choices are held fixed.
+
+#include <cuda_runtime.h>
+
+#include "gr_internal.h"
+
+namespace gr {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float go_min(float a, float b) {
+  // Go's min: NaN wins, -0 below +0
+  if (a != a || b != b) return __int_as_float(0x7fc00000);
+  if (a < b) return a;
+  if (b < a) return b;
+  return signbit(a) ? a : b;
+}
+__device__ __forceinline__ float go_max(float a, float b) {
+  if (a != a || b != b) return __int_as_float(0x7fc00000);
+  if (a > b) return a;
+  if (b > a) return b;
+  return signbit(a) ? b : a;
+}
+
+// Mesh.BoundingBox (mesh.go:28-51) of pos; min and max are order-free, so a
+// tree reduction gives the sequential loop's result.  One CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_diff_bbox(const float* __restrict__ pos, int nv, DevItem* items,
+                                                    int num_items) {
+  __shared__ float s_v[6][32];
+  __shared__ float s_b[32];
+  const int tid = threadIdx.x;
+  float mn[3] = {pos[0], pos[1], pos[2]}, mx[3] = {pos[0], pos[1], pos[2]};
+  for (int i = tid; i < nv; i += blockDim.x) {
+    const float4 p = reinterpret_cast<const float4*>(pos)[i];
+    mn[0] = go_min(mn[0], p.x); mn[1] = go_min(mn[1], p.y); mn[2] = go_min(mn[2], p.z);
+    mx[0] = go_max(mx[0], p.x); mx[1] = go_max(mx[1], p.y); mx[2] = go_max(mx[2], p.z);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = go_min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = go_max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  const int warp = tid >> 5, lane = tid & 31;
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) {
+      s_v[k][warp] = mn[k];
+      s_v[3 + k][warp] = mx[k];
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = lane < nw ? s_v[k][lane] : s_v[k][0];
+      mx[k] = lane < nw ? s_v[3 + k][lane] : s_v[3 + k][0];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = go_min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+        mx[k] = go_max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+      }
+    }
+    if (lane == 0) {
+      // corners in mesh.go's order: x outermost, then y, then z; w = 1
+      for (int c = 0; c < 8; ++c) {
+        s_b[4 * c + 0] = (c & 4) ? mx[0] : mn[0];
+        s_b[4 * c + 1] = (c & 2) ? mx[1] : mn[1];
+        s_b[4 * c + 2] = (c & 1) ? mx[2] : mn[2];
+        s_b[4 * c + 3] = 1.0f;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < num_items * 32; i += blockDim.x) items[i / 32].bbox[i % 32] = s_b[i % 32];
+}
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__device__ __forceinline__ float4 mvp_apply(const float* m, float4 v) {
+  float4 r;
+  r.x = m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3] * v.w;
+  r.y = m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7] * v.w;
+  r.z = m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11] * v.w;
+  r.w = m[12] * v.x + m[13] * v.y + m[14] * v.z + m[15] * v.w;
+  return r;
+}
+
+__global__ void __launch_bounds__(kThreads) k_diff_normals(const float* __restrict__ world,
+                                                           const float* __restrict__ vnrm, int nn, float* nhat) {
+  const int n = blockIdx.x * kThreads + threadIdx.x;
+  if (n >= nn) return;
+  const float4 v = mvp_apply(world, ldg4(vnrm + 4 * (size_t)n));
+  const float len = __fsqrt_rn(v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w);
+  reinterpret_cast<float4*>(nhat)[n] = make_float4(v.x / len, v.y / len, v.z / len, 0.0f);
+}
+
+// Geometry of one face at one pixel, shared by the forward and backward passes
+// so that both compute bit-identical values.
+struct FaceGeom {
+  int vi[3];
+  double A[3], B[3];  // d u_i / d p_i and d v_i / d p_i (xyz)
+  double u[3], v[3];
+  double D[3], T;     // b_i = D_i / T
+  bool ok;
+};
+
+__device__ __forceinline__ double dot4d(const double* q, float4 p) {
+  return __fma_rn(q[3], (double)p.w, __fma_rn(q[2], (double)p.z, __fma_rn(q[1], (double)p.y, q[0] * (double)p.x)));
+}
+
+__device__ __forceinline__ void face_geom(const DiffArgs& a, const DiffView& vw, int f, int px, int py,
+                                          FaceGeom& g) {
+  const int* vi = a.vidx + 3 * (size_t)f;
+  double A4[4], B4[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    A4[j] = __fma_rn(-(double)px, vw.Q[8 + j], vw.Q[j]);
+    B4[j] = __fma_rn(-(double)py, vw.Q[8 + j], vw.Q[4 + j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    g.A[j] = A4[j];
+    g.B[j] = B4[j];
+  }
+  g.ok = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    g.vi[k] = __ldg(vi + k);
+    const float4 p = ldg4(a.pos + 4 * (size_t)g.vi[k]);
+    g.ok = g.ok && dot4d(vw.Q + 8, p) < 0.0;  // W < 0: in front of the camera
+    g.u[k] = dot4d(A4, p);
+    g.v[k] = dot4d(B4, p);
+  }
+  g.D[0] = __fma_rn(g.u[1], g.v[2], -(g.u[2] * g.v[1]));
+  g.D[1] = __fma_rn(g.u[2], g.v[0], -(g.u[0] * g.v[2]));
+  g.D[2] = __fma_rn(g.u[0], g.v[1], -(g.u[1] * g.v[0]));
+  g.T = g.D[0] + g.D[1] + g.D[2];
+  g.ok = g.ok && g.T != 0.0 && isfinite(g.T);
+}
+
+struct Shade {
+  float l[3];
+  float c[3][3];    // vertex colours
+  float Ii[3];      // corner intensities
+  float col[3];     // interpolated colour
+  float I;
+  float4 t;         // texel
+  float4 out;
+};
+
+__device__ __forceinline__ void shade(const DiffArgs& a, const FaceGeom& g, float l0, float l1, uint32_t texel,
+                                      const int* ni, Shade& s) {
+  s.l[0] = l0;
+  s.l[1] = l1;
+  s.l[2] = 1.0f - l0 - l1;
+  s.I = 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) s.col[ch] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* cp = a.vcol + 3 * (size_t)g.vi[k];
+    const float4 n = ldg4(a.nhat + 4 * (size_t)__ldg(ni + k));
+    s.Ii[k] = 0.5f + 0.5f * (n.x * a.L[0] + n.y * a.L[1] + n.z * a.L[2]);
+    s.I += s.l[k] * s.Ii[k];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      s.c[k][ch] = __ldg(cp + ch);
+      s.col[ch] += s.l[k] * s.c[k][ch];
+    }
+  }
+  s.t = texel != kNoFace ? ldg4(a.tex + 4 * (size_t)texel) : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+  s.out = make_float4(s.I * s.col[0] * s.t.x, s.I * s.col[1] * s.t.y, s.I * s.col[2] * s.t.z, s.t.w);
+}
+
+__device__ __forceinline__ int wrap_index(float u, int n) {
+  const float f = floorf(u * (float)n);
+  if (!(f > -2.0e9f && f < 2.0e9f)) return 0;
+  int i = (int)f % n;
+  return i < 0 ? i + n : i;
+}
+
+// Block-wide sum of one double; thread 0 gets the result.
+__device__ __forceinline__ double block_sum(double v, double* s_red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) s_red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;
+}
+
+// Forward: per pixel record, shaded pixel and the loss.  Grid (pixels/256, views).
+__global__ void __launch_bounds__(kThreads) k_diff_shade(const DiffArgs a) {
+  __shared__ double s_red[kThreads / 32];
+  const DiffView& vw = a.views[blockIdx.y];
+  const int p = blockIdx.x * kThreads + threadIdx.x;
+  float lp = 0.0f;
+  if (p < vw.W * vw.H) {
+    const size_t gp = (size_t)vw.pix_base + (size_t)p;
+    const uint32_t gf = a.ids[gp];
+    DiffRecord rec{kNoFace, kNoFace, 0.0f, 0.0f};
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (gf != kNoFace) {
+      const int f = (int)(gf - vw.face_base);
+      FaceGeom g;
+      face_geom(a, vw, f, p % vw.W, p / vw.W, g);
+      if (g.ok) {
+        // the visibility pass snaps corners to whole pixels, so a pixel may lie
+        // just outside the unsnapped face: clip its barycentrics to the face
+        const double iT = 1.0 / g.T;
+        const double m0 = fmax(g.D[0] * iT, 0.0), m1 = fmax(g.D[1] * iT, 0.0), m2 = fmax(g.D[2] * iT, 0.0);
+        const double ims = 1.0 / (m0 + m1 + m2);
+        const float l0 = (float)(m0 * ims), l1 = (float)(m1 * ims);
+        uint32_t texel = kNoFace;
+        if (a.tex && a.uv) {
+          const float l2 = 1.0f - l0 - l1;
+          const float* uv = a.uv + 6 * (size_t)f;
+          const float u = l0 * __ldg(uv) + l1 * __ldg(uv + 2) + l2 * __ldg(uv + 4);
+          const float v = l0 * __ldg(uv + 1) + l1 * __ldg(uv + 3) + l2 * __ldg(uv + 5);
+          texel = (uint32_t)(wrap_index(v, a.th) * a.tw + wrap_index(u, a.tw));
+        }
+        Shade s;
+        shade(a, g, l0, l1, texel, a.nidx + 3 * (size_t)f, s);
+        out = s.out;
+        rec = DiffRecord{gf, texel, l0, l1};
+      }
+    }
+    a.rec[gp] = rec;
+    if (a.image) reinterpret_cast<float4*>(a.image)[gp] = out;
+    const float4 tg = reinterpret_cast<const float4*>(a.target)[gp];
+    const float dx = out.x - tg.x, dy = out.y - tg.y, dz = out.z - tg.z, dw = out.w - tg.w;
+    lp = dx * dx + dy * dy + dz * dz + dw * dw;
+  }
+  const double t = block_sum((double)lp, s_red);
+  if (threadIdx.x == 0 && t != 0.0) atomicAdd(a.loss, t);
+}
+
+// Backward: gradients of the loss of the last forward pass.
+__global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
+  __shared__ double s_red[kThreads / 32];
+  const DiffView& vw = a.views[blockIdx.y];
+  const int p = blockIdx.x * kThreads + threadIdx.x;
+  float gl[3] = {0.0f, 0.0f, 0.0f};
+  if (p < vw.W * vw.H) {
+    const size_t gp = (size_t)vw.pix_base + (size_t)p;
+    const DiffRecord rec = a.rec[gp];
+    if (rec.face != kNoFace) {
+      const int f = (int)(rec.face - vw.face_base);
+      FaceGeom g;
+      face_geom(a, vw, f, p % vw.W, p / vw.W, g);
+      const int* ni = a.nidx + 3 * (size_t)f;
+      Shade s;
+      shade(a, g, rec.l0, rec.l1, rec.texel, ni, s);
+      const float4 tg = reinterpret_cast<const float4*>(a.target)[gp];
+      const float go[4] = {2.0f * (s.out.x - tg.x), 2.0f * (s.out.y - tg.y), 2.0f * (s.out.z - tg.z),
+                           2.0f * (s.out.w - tg.w)};
+      const float t3[3] = {s.t.x, s.t.y, s.t.z};
+      // texels
+      if (rec.texel != kNoFace) {
+        float* gt = a.g_tex + 4 * (size_t)rec.texel;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) atomicAdd(gt + ch, go[ch] * s.I * s.col[ch]);
+        atomicAdd(gt + 3, go[3]);
+      }
+      // vertex colours, and d loss / d intensity
+      float dI = 0.0f;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) dI += go[ch] * s.col[ch] * t3[ch];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float* gc = a.g_vcol + 3 * (size_t)g.vi[k];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) atomicAdd(gc + ch, go[ch] * s.I * t3[ch] * s.l[k]);
+      }
+      // light: dI/dL = sum_k l_k 0.5 nhat_k
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float4 n = ldg4(a.nhat + 4 * (size_t)__ldg(ni + k));
+        const float w = dI * 0.5f * s.l[k];
+        gl[0] += w * n.x;
+        gl[1] += w * n.y;
+        gl[2] += w * n.z;
+      }
+      // positions through the barycentrics: G_k = d loss / d l_k
+      float G[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float gk = dI * s.Ii[k];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) gk += go[ch] * s.I * t3[ch] * s.c[k][ch];
+        G[k] = gk;
+      }
+      // l_k = m_k / sum m, m_k = max(b_k, 0), b_k = D_k / T (double precision)
+      const double iT = 1.0 / g.T;
+      double b[3], m[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        b[k] = g.D[k] * iT;
+        m[k] = fmax(b[k], 0.0);
+      }
+      const double ims = 1.0 / (m[0] + m[1] + m[2]);
+      const double Gl = (double)G[0] * (m[0] * ims) + (double)G[1] * (m[1] * ims) + (double)G[2] * (m[2] * ims);
+      double Gb[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Gb[k] = b[k] > 0.0 ? ((double)G[k] - Gl) * ims : 0.0;
+      const double Gbb = Gb[0] * b[0] + Gb[1] * b[1] + Gb[2] * b[2];
+      double dD[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dD[k] = (Gb[k] - Gbb) * iT;
+      // D_0 = u1 v2 - u2 v1, D_1 = u2 v0 - u0 v2, D_2 = u0 v1 - u1 v0
+      const double gu[3] = {dD[2] * g.v[1] - dD[1] * g.v[2], dD[0] * g.v[2] - dD[2] * g.v[0],
+                            dD[1] * g.v[0] - dD[0] * g.v[1]};
+      const double gv[3] = {dD[1] * g.u[2] - dD[2] * g.u[1], dD[2] * g.u[0] - dD[0] * g.u[2],
+                            dD[0] * g.u[1] - dD[1] * g.u[0]};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float* gp4 = a.g_pos + 4 * (size_t)g.vi[k];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) atomicAdd(gp4 + j, (float)(gu[k] * g.A[j] + gv[k] * g.B[j]));
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double t = block_sum((double)gl[j], s_red);
+    if (threadIdx.x == 0 && t != 0.0) atomicAdd(a.g_light + j, t);
+  }
+}
+
+}  // namespace
+
+int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, void* stream) {
+  if (nv <= 0 || num_items <= 0) return 0;
+  k_diff_bbox<<<1, 1024, 0, (cudaStream_t)stream>>>(pos, nv, items, num_items);
+  return (int)cudaGetLastError();
+}
+
+int launch_diff_normals(const float* world, const float* vnrm, int nn, float* nhat, void* stream) {
+  if (nn <= 0) return 0;
+  k_diff_normals<<<(nn + kThreads - 1) / kThreads, kThreads, 0, (cudaStream_t)stream>>>(world, vnrm, nn, nhat);
+  return (int)cudaGetLastError();
+}
+
+int launch_diff_forward(const DiffArgs& a, void* stream) {
+  const dim3 grid((unsigned)((a.max_pixels + kThreads - 1) / kThreads), (unsigned)a.num_views);
+  k_diff_shade<<<grid, kThreads, 0, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int launch_diff_backward(const DiffArgs& a, void* stream) {
+  const dim3 grid((unsigned)((a.max_pixels + kThreads - 1) / kThreads), (unsigned)a.num_views);
+  k_diff_grad<<<grid, kThreads, 0, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace gr

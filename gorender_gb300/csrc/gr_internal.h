@@ -161,6 +161,54 @@ struct FrameArgs {
   int raster_ctas;                  // persistent raster grid
 };
 
+// View flag (internal, never set by callers): the raster resolve writes the
+// winning face's global index (or kNoFace) into out_rgba instead of a colour.
+constexpr uint32_t kViewFaceIds = 0x80000000u;
+constexpr uint32_t kNoFace = 0xFFFFFFFFu;
+
+// ---- differentiable shading (an extension with no counterpart in the reference) ----
+// One view of the differentiable object.
+struct DiffView {
+  double Q[12];                     // rows 0 and 1 of S * MVP, then row 3 of MVP (clip W)
+  int W, H;
+  uint32_t pix_base;                // first pixel of this view in the per-pixel buffers
+  uint32_t face_base;               // first global face index of this view's item
+};
+
+// Per-pixel forward record: the visible face (or kNoFace), the texel it
+// sampled (or kNoFace without a texture) and two perspective-correct
+// barycentrics (the third is 1 - l0 - l1).
+struct DiffRecord {
+  uint32_t face;
+  uint32_t texel;
+  float l0, l1;
+};
+
+struct DiffArgs {
+  const DiffView* views;
+  int num_views;
+  int max_pixels;                   // largest view (grid x extent)
+  int nv, nf, nn;
+  const float* pos;                 // nv x 4 (parameter)
+  const float* vcol;                // nv x 3 (parameter)
+  const float* tex;                 // th x tw x 4 RGBA (parameter; may be null)
+  int tw, th;
+  float L[4];                       // light direction (parameter)
+  const int* vidx;                  // nf x 3
+  const int* nidx;                  // nf x 3
+  const float* uv;                  // nf x 6 (may be null)
+  const float* nhat;                // nn x 4: normalised world-space vertex normals
+  const uint32_t* ids;              // per pixel: global face index or kNoFace (raster output)
+  DiffRecord* rec;                  // per pixel
+  const float* target;              // per pixel RGBA
+  float* image;                     // per pixel RGBA (may be null)
+  double* loss;                     // one value, accumulated
+  float* g_pos;                     // nv x 4 (w left 0)
+  float* g_vcol;                    // nv x 3
+  float* g_tex;                     // th x tw x 4
+  double* g_light;                  // 3, accumulated
+};
+
 // Kernel launchers (gr_kernels.cu).
 // events (optional): 4 cudaEvent_t recorded before k_project, after k_project,
 // after k_bin_big and after k_raster.
@@ -168,6 +216,14 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
 
 // Persistent raster grid: SMs x resident CTAs of k_raster<TS> x waves.
 int raster_grid(int tile_shift, int waves);
+
+// Differentiable path (gr_diff.cu).
+// Writes the bounding box (Mesh.BoundingBox layout) of pos into each item's bbox.
+int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, void* stream);
+// nhat[n] = xyz of Vec4.Normalize(world * vnrm[n]) (renderer.go:328-331), w = 0.
+int launch_diff_normals(const float* world, const float* vnrm, int nn, float* nhat, void* stream);
+int launch_diff_forward(const DiffArgs& a, void* stream);
+int launch_diff_backward(const DiffArgs& a, void* stream);
 
 // Records a message for gr_last_error() on this thread and returns code (gr_api.cpp).
 int32_t set_error(int32_t code, const char* fmt, ...);

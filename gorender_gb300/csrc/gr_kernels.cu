@@ -1177,20 +1177,26 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     for (int j = 0; j < 4; ++j) {
       const int x = tx0 + col + j;
       const unsigned long long k = keys[j];
+      const bool face_ids = vw.flags & kViewFaceIds;
       if (k == BG_KEY || x > tx1) {
         const bool dot = (x % 10 == 0) && (y % 10 == 0) && x >= 10 && y >= 10;  // DotGrid
-        out_c[j] = dot ? 0xFF646464u : 0xFF323232u;
+        out_c[j] = face_ids ? kNoFace : dot ? 0xFF646464u : 0xFF323232u;
         out_z[j] = -1.0f;
         continue;
       }
       const uint32_t okey = (uint32_t)k & 0x7FFFFFFFu;
       const uint32_t r = a.rec_of_key[okey];
       const TriRaster t = a.rast[r];
-      const TriShade s = a.shade[r];
       bool inside;
       float e12f, e20f, al, be, ga;
       edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
       const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
+      if (face_ids) {
+        out_c[j] = (okey - 1u) / (uint32_t)kKeysPerFace;  // the face of order key face * 8 + fan + 1
+        out_z[j] = z;
+        continue;
+      }
+      const TriShade s = a.shade[r];
       const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
       uint32_t c;
       if (s.tex >= 0) {

@@ -443,3 +443,78 @@ def draw_views(ctx: Context, views, entries) -> None:
     for i, (_, _, _, v) in enumerate(entries):
         items[i].reserved = v
     N.check(N.lib().gr_draw_views(ctx.handle, vs, len(views), items, len(entries)))
+
+
+# ---- differentiable forward/backward (extension) ----
+
+def diff_views(scene) -> Tuple[np.ndarray, list]:
+    """(world matrix, [(width, height, flags, screen16, mvp16)]) of a scenes.DiffSceneData,
+    with the host matrix code (matrix.go restated in the library)."""
+    fov = fov_radians(scene.fov_deg)
+    sm = screen_matrix(scene.width, scene.height)
+    views, world = [], None
+    for cam in scene.cameras:
+        mvp, world = object_matrices((1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), cam.position,
+                                     cam.direction, cam.up, scene.width, scene.height, fov)
+        views.append((scene.width, scene.height, scene.flags, sm, mvp))
+    return world, views
+
+
+class Diff:
+    """gr_diff_*: differentiable shading of one mesh over several views.
+
+    Parameters, targets, images and gradients are device pointers (ints):
+    ``forward(pos, vcol, tex, light, target, image=None) -> loss`` and
+    ``backward(g_pos, g_vcol, g_tex) -> light gradient``."""
+
+    def __init__(self, ctx: Context, mesh: int, world, views, tex_size: Tuple[int, int] = (0, 0)):
+        self.ctx = ctx
+        vs = (N.DiffView * len(views))()
+        for i, (w, h, flags, sm, mvp) in enumerate(views):
+            vs[i].width, vs[i].height, vs[i].flags = w, h, flags
+            for k in range(16):
+                vs[i].screen[k] = float(sm[k])
+                vs[i].mvp[k] = float(mvp[k])
+        wm = np.ascontiguousarray(world, np.float32)
+        self._h = C.c_void_p()
+        N.check(N.lib().gr_diff_create(ctx.handle, mesh, _fp(wm), int(tex_size[1]), int(tex_size[0]), vs,
+                                       len(views), C.byref(self._h)))
+        self.nviews = len(views)
+        ctx._batches.append(self)
+
+    def forward(self, pos, vcol, tex, light, target, image=None) -> float:
+        p = N.DiffParams()
+        p.positions, p.vertex_colors = int(pos), int(vcol)
+        p.texture = None if tex is None else int(tex)
+        for k in range(3):
+            p.light[k] = float(light[k])
+        loss = C.c_double()
+        N.check(N.lib().gr_diff_forward(self._h, C.byref(p), int(target), None if image is None else int(image),
+                                        C.byref(loss)))
+        return float(loss.value)
+
+    def backward(self, g_pos, g_vcol, g_tex=None) -> np.ndarray:
+        g = N.DiffGrads()
+        g.positions, g.vertex_colors = int(g_pos), int(g_vcol)
+        g.texture = None if g_tex is None else int(g_tex)
+        N.check(N.lib().gr_diff_backward(self._h, C.byref(g)))
+        return np.array(g.light[:], np.float64)
+
+    def buffers(self):
+        """(face ids device pointer, records device pointer, pixels)."""
+        ids, rec, n = C.c_void_p(), C.c_void_p(), C.c_int64()
+        N.check(N.lib().gr_diff_buffers(self._h, C.byref(ids), C.byref(rec), C.byref(n)))
+        return ids.value, rec.value, int(n.value)
+
+    def close(self):
+        if self._h:
+            N.lib().gr_diff_destroy(self._h)
+            self._h = C.c_void_p()
+        if self in self.ctx._batches:
+            self.ctx._batches.remove(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -447,3 +447,63 @@ def multiview_batch(count: int = 256, seed: int = 0, min_tris: int = 100, max_tr
         flags = DEFAULT_FLAGS | (FLAT_SHADING if material == 0 else 0)
         out.append(SceneData(f"view{k}", w, h, [ObjectData(m)], cam, textures, flags))
     return out
+
+
+@dataclasses.dataclass
+class DiffSceneData:
+    """One mesh seen from several cameras, with the parameters of the
+    differentiable shading model and a perturbed copy that renders the target."""
+
+    mesh: MeshData
+    cameras: List[CameraData]
+    width: int
+    height: int
+    vcol: np.ndarray       # nv x 3
+    tex: np.ndarray        # th x tw x 4
+    light: np.ndarray      # 3
+    target_params: dict    # pos, vcol, tex, light perturbed by N(0, sigma)
+    flags: int = FRUSTUM_CLIPPING | SHOW_FACES | BACKFACE_CULLING
+    fov_deg: float = 60.0
+
+    @property
+    def num_views(self) -> int:
+        return len(self.cameras)
+
+
+def spherical_uvs(m: MeshData) -> np.ndarray:
+    """Per-corner UVs from the direction of each corner (u from the azimuth, v from the height)."""
+    p = m.pos[m.vidx.reshape(-1), :3].astype(np.float64)
+    u = (np.arctan2(p[:, 2], p[:, 0]) / (2 * math.pi) + 0.5).astype(np.float32)
+    v = (p[:, 1] / np.sqrt((p * p).sum(axis=1)) * 0.5 + 0.5).astype(np.float32)
+    return np.stack([u, v], axis=1).reshape(-1, 6).astype(np.float32)
+
+
+def diff_scene(views: int = 64, size: int = 512, level: int = 6, tex_size: int = 256, seed: int = 0,
+               sigma: float = 0.05, radius: float = 3.0) -> DiffSceneData:
+    """The differentiable forward+backward workload: an icosphere (20 * 4^level
+    faces) with +-5% radial noise, vertex normals, spherical UVs, vertex RGB in
+    U[0,1], a tex_size^2 RGBA fp32 texture in U[0,1] and the reference's light
+    direction; cameras on a sphere of the given radius looking at the origin.
+    The target parameters add N(0, sigma) to positions, colours, texels and
+    the light."""
+    rng = SplitMix64(seed)
+    m = icosphere(level, noise=0.05, seed=seed, normals=True)
+    m.uv = spherical_uvs(m)
+    cams = []
+    d = rng.normal(3 * views).astype(np.float64).reshape(views, 3)
+    for k in range(views):
+        n = math.sqrt(float((d[k] * d[k]).sum())) or 1.0
+        pos = tuple(float(x) for x in (d[k] / n * radius))
+        up = (0.0, 1.0, 0.0) if abs(d[k][1] / n) < 0.95 else (1.0, 0.0, 0.0)
+        cams.append(CameraData(pos, tuple(-x for x in pos), up))
+    vcol = rng.uniform(3 * m.nv).astype(np.float32).reshape(m.nv, 3)
+    tex = rng.uniform(4 * tex_size * tex_size).astype(np.float32).reshape(tex_size, tex_size, 4)
+    light = np.array([-1.0, 1.0, 1.0], np.float64)
+    light = (light / math.sqrt(3.0)).astype(np.float32)
+    pos_t = m.pos.copy()
+    pos_t[:, :3] += rng.normal(3 * m.nv, sigma).astype(np.float32).reshape(m.nv, 3)
+    target = {"pos": pos_t,
+              "vcol": (vcol + rng.normal(vcol.size, sigma).astype(np.float32).reshape(vcol.shape)),
+              "tex": (tex + rng.normal(tex.size, sigma).astype(np.float32).reshape(tex.shape)),
+              "light": (light + rng.normal(3, sigma).astype(np.float32))}
+    return DiffSceneData(m, cams, size, size, vcol, tex, light, target)

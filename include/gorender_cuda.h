@@ -294,6 +294,72 @@ int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* objects, int32_
                         const gr_frame_params* params, uint8_t* rgba_dev, float* z_dev, void* stream,
                         int64_t* tpf_out);
 
+/* ---- differentiable forward/backward ----
+ * An extension with no counterpart in the reference renderer.  Visibility is
+ * the exact frame pipeline's (the face FrameBuffer.Triangle leaves at each
+ * pixel, rasterizer.go:90-183, with culling and clipping as the view flags
+ * say); over it a smooth shading model is differentiated:
+ *   l_i  perspective-correct barycentrics of pixel (x, y) from the unsnapped
+ *        screen positions S * (clip_i / W_i) of the visible face's corners,
+ *        clipped to the face (negative ones set to 0, the rest renormalised:
+ *        visibility snaps corners to whole pixels, so a pixel can lie just
+ *        outside the unsnapped face)
+ *   c    = sum l_i c_i                  vertex RGB (parameter)
+ *   I    = sum l_i (0.5 + 0.5 n_i . L)  n_i = xyz of Vec4.Normalize(world * vertex
+ *                                       normal) (renderer.go:328-331), L a parameter
+ *   t    = texel at (floor(v th) mod th, floor(u tw) mod tw), (u, v) = sum l_i uv_i
+ *   out  = (I c_r t_r, I c_g t_g, I c_b t_b, t_a)   (t = 1 without UVs)
+ *   loss = sum over views, pixels and channels of (out - target)^2
+ * Gradients of the loss with respect to vertex colours, texels, the light and
+ * vertex positions are exact for fixed visibility and texel choices (position
+ * gradients flow through the barycentrics only).  Faces with a corner at or
+ * behind the camera plane (W >= 0) are not shaded (out = 0, no gradient).
+ * Per-pixel buffers hold all views back to back, view v starting at the sum
+ * of the earlier views' W * H pixels. */
+typedef struct {
+  int32_t width, height;
+  uint32_t flags;          /* GR_FRUSTUM_CLIPPING / GR_BACKFACE_CULLING for visibility;
+                              shading flags are ignored */
+  int32_t reserved;
+  float screen[16];        /* NewScreenMatrix(width, height) */
+  float mvp[16];           /* I*P*V*W of the object in this view */
+} gr_diff_view;
+
+typedef struct {
+  const float* positions;      /* DEVICE num_vertices x 4 (w = 1); visibility uses them too */
+  const float* vertex_colors;  /* DEVICE num_vertices x 3 */
+  const float* texture;        /* DEVICE texture_height x texture_width x 4 RGBA, or NULL */
+  float light[3];
+  int32_t reserved;
+} gr_diff_params;
+
+typedef struct {
+  float* positions;      /* DEVICE num_vertices x 4 (w gradient 0), overwritten */
+  float* vertex_colors;  /* DEVICE num_vertices x 3, overwritten */
+  float* texture;        /* DEVICE texture_height x texture_width x 4, overwritten (or NULL) */
+  double light[3];       /* written */
+} gr_diff_grads;
+
+typedef struct gr_diff gr_diff;
+
+/* One mesh (it needs vertex normals with normal indices; UVs optional) seen in
+ * num_views views with one world matrix (host, 16 floats). */
+int32_t gr_diff_create(gr_context* ctx, int32_t mesh, const float* world, int32_t texture_width,
+                       int32_t texture_height, const gr_diff_view* views, int32_t num_views, gr_diff** out);
+/* Renders the views with params, writes the per-pixel records (and the image,
+ * RGBA fp32 per pixel, when image_dev is not NULL) and returns the loss
+ * against target_dev (RGBA fp32 per pixel).  params and target must stay
+ * unchanged until the matching gr_diff_backward. */
+int32_t gr_diff_forward(gr_diff* d, const gr_diff_params* params, const float* target_dev, float* image_dev,
+                        double* loss);
+/* Gradients of the last forward's loss. */
+int32_t gr_diff_backward(gr_diff* d, gr_diff_grads* grads);
+/* Device buffers of the last forward: per pixel the visible face index
+ * (view v's faces are v * num_faces + f; 0xFFFFFFFF = none) and a 16-byte
+ * record {face, texel (y * width + x, or 0xFFFFFFFF), l0, l1}; pixels = total. */
+int32_t gr_diff_buffers(gr_diff* d, const uint32_t** face_ids, const void** records, int64_t* pixels);
+int32_t gr_diff_destroy(gr_diff* d);
+
 #ifdef __cplusplus
 }
 #endif

@@ -436,12 +436,13 @@ typedef struct {
   float col[3][3];
   int32_t tex;      /* -1 = nil */
   int32_t has_col;  /* per-vertex RGB extension active */
+  uint32_t face;    /* global face index: earlier objects' faces + face index */
 } RTri;
 
 /* FrameBuffer.Triangle (rasterizer.go:90-183) restricted to rows
  * [band_y0, band_y1).  With the full band this is the reference loop.  The
  * per-vertex colour extension replaces faceColor by the interpolated RGB. */
-static void raster_tri(uint8_t* rgba, float* zb, int32_t width, int32_t height, const RTri* t,
+static void raster_tri(uint8_t* rgba, float* zb, uint32_t* ids, int32_t width, int32_t height, const RTri* t,
                        int64_t tsx, int64_t tsy, int64_t tex_, int64_t tey,
                        const orc_texture* texture, int64_t band_y0, int64_t band_y1) {
   int64_t x0 = t->x[0], y0 = t->y[0], x1 = t->x[1], y1 = t->y[1], x2 = t->x[2], y2 = t->y[2];
@@ -495,11 +496,13 @@ static void raster_tri(uint8_t* rgba, float* zb, int32_t width, int32_t height, 
             c[3] = 255;
             zb[index] = zRec;
             memcpy(rgba + 4 * index, c, 4);
+            if (ids) ids[index] = t->face;
             goto next;
           } else {
             memcpy(c, kFaceColor, 4);
           }
           zb[index] = zRec;
+          if (ids) ids[index] = t->face;
           /* colorIntensity (rasterizer.go:81-88) */
           rgba[4 * index + 0] = orc_go_uint8((float)c[0] * intensity);
           rgba[4 * index + 1] = orc_go_uint8((float)c[1] * intensity);
@@ -531,7 +534,7 @@ void orc_fb_triangle(uint8_t* rgba, float* z, int32_t width, int32_t height,
   t.x[2] = x2; t.y[2] = y2; t.w[2] = z2; t.u[2] = u2; t.v[2] = v2;
   t.in[0] = ia; t.in[1] = ib; t.in[2] = ic;
   t.tex = -1;
-  raster_tri(rgba, z, width, height, &t, tsx, tsy, tex_, tey, texture, INT64_MIN, INT64_MAX);
+  raster_tri(rgba, z, NULL, width, height, &t, tsx, tsy, tex_, tey, texture, INT64_MIN, INT64_MAX);
 }
 
 /* ------------------------------------------------------------------ */
@@ -571,7 +574,7 @@ static inline V4 ld4(const float* p) { V4 v = {p[0], p[1], p[2], p[3]}; return v
 
 /* projectObject (renderer.go:254-407) for one item, appending binned
  * triangles in face order.  Sequential mode: one tile spanning the screen. */
-static int project_object(const orc_item* it, const orc_frame* fr, TriList* out) {
+static int project_object(const orc_item* it, const orc_frame* fr, uint32_t face_base, TriList* out) {
   const orc_mesh* m = it->mesh;
   const uint32_t fl = fr->flags;
   const float znear = 0.0f, zfar = 50.0f;   /* renderer.go:121 */
@@ -667,6 +670,7 @@ static int project_object(const orc_item* it, const orc_frame* fr, TriList* out)
       }
       t.tex = tex;
       t.has_col = m->vcolor != NULL;
+      t.face = face_base + (uint32_t)fi;
       int e = tl_push(out, &t);
       if (e) return e;
     }
@@ -688,6 +692,8 @@ typedef struct {
   pthread_mutex_t mu;
   uint8_t* rgba;
   float* z;
+  uint32_t* ids;          /* optional: face that wrote each pixel */
+  uint32_t* face_base;    /* per item */
   int32_t nthreads;
   int32_t band;           /* band index for the raster phase */
 } DrawCtx;
@@ -702,7 +708,7 @@ static void raster_band(DrawCtx* c, int64_t y0, int64_t y1) {
       const RTri* t = &l->v[k];
       const orc_texture* tx = NULL;
       if ((fl & ORC_SHOW_TEXTURES) && t->tex >= 0) tx = &fr->textures[t->tex];  /* renderer.go:176-178 */
-      raster_tri(c->rgba, c->z, fr->width, fr->height, t, 0, 0, fr->width, fr->height, tx, y0, y1);
+      raster_tri(c->rgba, c->z, c->ids, fr->width, fr->height, t, 0, 0, fr->width, fr->height, tx, y0, y1);
     }
   }
 }
@@ -714,7 +720,7 @@ static void* project_worker(void* arg) {
     int32_t i = c->next++;
     pthread_mutex_unlock(&c->mu);
     if (i >= c->nitems) break;
-    c->errs[i] = project_object(&c->items[i], c->fr, &c->lists[i]);
+    c->errs[i] = project_object(&c->items[i], c->fr, c->face_base[i], &c->lists[i]);
   }
   return NULL;
 }
@@ -732,7 +738,7 @@ int64_t orc_project(const orc_item* items, int32_t nitems, const orc_frame* fr, 
   int64_t n = 0;
   for (int32_t i = 0; i < nitems; i++) {
     TriList l = {0, 0, 0};
-    int e = project_object(&items[i], fr, &l);
+    int e = project_object(&items[i], fr, 0u, &l);
     if (e) { free(l.v); return e; }
     for (int64_t k = 0; k < l.n; k++, n++) {
       if (n >= cap) continue;
@@ -749,7 +755,14 @@ int64_t orc_project(const orc_item* items, int32_t nitems, const orc_frame* fr, 
 
 int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr, uint8_t* rgba, float* z,
              int64_t* tpf, int32_t nthreads) {
+  return orc_draw_ids(items, nitems, fr, rgba, z, NULL, tpf, nthreads);
+}
+
+int orc_draw_ids(const orc_item* items, int32_t nitems, const orc_frame* fr, uint8_t* rgba, float* z,
+                 uint32_t* ids, int64_t* tpf, int32_t nthreads) {
   const int64_t npx = (int64_t)fr->width * fr->height;
+  if (ids)
+    for (int64_t i = 0; i < npx; i++) ids[i] = 0xFFFFFFFFu;
   /* FrameBuffer.Clear (rasterizer.go:36-44) and DotGrid (rasterizer.go:46-52) */
   for (int64_t i = 0; i < npx; i++) {
     rgba[4 * i] = 50; rgba[4 * i + 1] = 50; rgba[4 * i + 2] = 50; rgba[4 * i + 3] = 255;
@@ -765,16 +778,18 @@ int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr, uint8_t
 
   DrawCtx c;
   memset(&c, 0, sizeof(c));
-  c.items = items; c.nitems = nitems; c.fr = fr; c.rgba = rgba; c.z = z;
+  c.items = items; c.nitems = nitems; c.fr = fr; c.rgba = rgba; c.z = z; c.ids = ids;
   c.lists = (TriList*)calloc((size_t)(nitems > 0 ? nitems : 1), sizeof(TriList));
   c.errs = (int*)calloc((size_t)(nitems > 0 ? nitems : 1), sizeof(int));
-  if (!c.lists || !c.errs) { free(c.lists); free(c.errs); return -4; }
+  c.face_base = (uint32_t*)calloc((size_t)(nitems > 0 ? nitems : 1), sizeof(uint32_t));
+  if (!c.lists || !c.errs || !c.face_base) { free(c.lists); free(c.errs); free(c.face_base); return -4; }
+  for (int32_t i = 1; i < nitems; i++) c.face_base[i] = c.face_base[i - 1] + (uint32_t)items[i - 1].mesh->nf;
   pthread_mutex_init(&c.mu, NULL);
   if (nthreads < 1) nthreads = 1;
 
   /* Phase 1: projection, one task per object (renderer.go:451-459). */
   if (nthreads == 1 || nitems <= 1) {
-    for (int32_t i = 0; i < nitems; i++) c.errs[i] = project_object(&items[i], fr, &c.lists[i]);
+    for (int32_t i = 0; i < nitems; i++) c.errs[i] = project_object(&items[i], fr, c.face_base[i], &c.lists[i]);
   } else {
     int nt = nthreads < nitems ? nthreads : nitems;
     pthread_t th[256];
@@ -811,6 +826,7 @@ int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr, uint8_t
   for (int32_t i = 0; i < nitems; i++) free(c.lists[i].v);
   free(c.lists);
   free(c.errs);
+  free(c.face_base);
   pthread_mutex_destroy(&c.mu);
   return err;
 }

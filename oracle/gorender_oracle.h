@@ -93,6 +93,46 @@ typedef struct {
 int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr,
              uint8_t* rgba, float* z, int64_t* tpf, int32_t nthreads);
 
+/* orc_draw that also records, per pixel, the global face index (faces of
+ * earlier items first) of the triangle that last wrote it, or 0xFFFFFFFF. */
+int orc_draw_ids(const orc_item* items, int32_t nitems, const orc_frame* fr,
+                 uint8_t* rgba, float* z, uint32_t* ids, int64_t* tpf, int32_t nthreads);
+
+/* ---- differentiable shading extension (no counterpart in the reference) ----
+ * FP64 restatement of the shading model the CUDA differentiable path
+ * implements over fixed visibility (per-pixel face ids) and, optionally,
+ * fixed texel choices.  Inputs are doubles so that finite differences can be
+ * taken without float32 rounding of the perturbed parameter. */
+typedef struct {
+  int32_t nv, nf, nn;
+  const double* pos;      /* nv x 4 (w = 1) */
+  const double* vcol;     /* nv x 3 */
+  const int32_t* vidx;    /* nf x 3 */
+  const int32_t* nidx;    /* nf x 3 */
+  const double* vnrm;     /* nn x 4 */
+  const double* uv;       /* nf x 6, or NULL */
+  const double* tex;      /* th x tw x 4, or NULL */
+  int32_t tw, th;
+  double light[3];
+  double world[16];
+} orc_diff_scene;
+
+typedef struct {
+  int32_t width, height;
+  double screen[16];
+  double mvp[16];
+} orc_diff_view;
+
+/* Loss of the views (pixels back to back) against target (RGBA per pixel).
+ * ids: visible global face per pixel (view v's faces are v * nf + f).
+ * texel_in: texel per pixel to use (NULL: choose from the UVs, writing the
+ * choice to texel_out when that is not NULL).  image, g_pos (nv x 4),
+ * g_vcol (nv x 3), g_tex (th x tw x 4) and g_light (3) are optional outputs;
+ * gradients are written (not accumulated).  Returns the loss. */
+double orc_diff_eval(const orc_diff_scene* s, const orc_diff_view* views, int32_t nviews, const uint32_t* ids,
+                     const uint32_t* texel_in, uint32_t* texel_out, const float* target, double* image,
+                     double* g_pos, double* g_vcol, double* g_tex, double* g_light);
+
 /* Projection only: the binned triangles of every item in draw order, as
  * drawProjection passes them to FrameBuffer.Triangle (int x, int y per
  * vertex into xy_out, 6 per triangle; clip W into w_out, 3 per triangle).

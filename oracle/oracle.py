@@ -18,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 SRC = os.path.join(HERE, "gorender_oracle.c")
+SOURCES = [SRC, os.path.join(HERE, "gorender_diff.c")]
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread", "-Wall"]
 
@@ -25,9 +26,9 @@ CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pt
 def build(force: bool = False) -> str:
     """Compile the restatement with contraction disabled (gcc, any host arch)."""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "gorender_oracle.h"))):
+            [os.path.getmtime(f) for f in SOURCES] + [os.path.getmtime(os.path.join(HERE, "gorender_oracle.h"))]):
         tmp = LIB_PATH + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"])
+        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, *SOURCES, "-lm"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -42,6 +43,18 @@ class Mesh(C.Structure):
                 ("fnrm", C.c_void_p), ("vidx", C.c_void_p), ("nidx", C.c_void_p),
                 ("uv", C.c_void_p), ("tex", C.c_void_p), ("vcolor", C.c_void_p),
                 ("nf", C.c_int32), ("bbox", C.c_float * 32)]
+
+
+class DiffScene(C.Structure):
+    _fields_ = [("nv", C.c_int32), ("nf", C.c_int32), ("nn", C.c_int32), ("pos", C.c_void_p),
+                ("vcol", C.c_void_p), ("vidx", C.c_void_p), ("nidx", C.c_void_p), ("vnrm", C.c_void_p),
+                ("uv", C.c_void_p), ("tex", C.c_void_p), ("tw", C.c_int32), ("th", C.c_int32),
+                ("light", C.c_double * 3), ("world", C.c_double * 16)]
+
+
+class DiffView(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("screen", C.c_double * 16),
+                ("mvp", C.c_double * 16)]
 
 
 class Item(C.Structure):
@@ -67,6 +80,13 @@ def lib():
         L.orc_draw.argtypes = [C.POINTER(Item), C.c_int32, C.POINTER(Frame), C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_int64), C.c_int32]
         L.orc_draw.restype = C.c_int
+        L.orc_draw_ids.argtypes = [C.POINTER(Item), C.c_int32, C.POINTER(Frame), C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.POINTER(C.c_int64), C.c_int32]
+        L.orc_draw_ids.restype = C.c_int
+        L.orc_diff_eval.argtypes = [C.POINTER(DiffScene), C.POINTER(DiffView), C.c_int32, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]
+        L.orc_diff_eval.restype = C.c_double
         L.orc_project.argtypes = [C.POINTER(Item), C.c_int32, C.POINTER(Frame), C.c_void_p, C.c_void_p, C.c_int64]
         L.orc_project.restype = C.c_int64
         L.orc_transform_batch.argtypes = [fp, fp, C.c_int64]
@@ -290,8 +310,9 @@ def project_scene(scene, flags=None, light=None, items_override=None):
 
 
 def draw_scene(scene, nthreads: int = 1, flags: Optional[int] = None, light=None,
-               items_override: Optional[Sequence[Tuple[np.ndarray, np.ndarray]]] = None):
-    """Render a scenes.SceneData with the oracle.  Returns (rgba HxWx4, z HxW, tpf, status)."""
+               items_override: Optional[Sequence[Tuple[np.ndarray, np.ndarray]]] = None, face_ids: bool = False):
+    """Render a scenes.SceneData with the oracle.  Returns (rgba HxWx4, z HxW, tpf, status), plus the
+    per-pixel face ids (uint32 HxW) when face_ids is set."""
     keep = _Keep()
     fov = fov_radians(scene.fov_deg)
     meshes = {}
@@ -326,6 +347,82 @@ def draw_scene(scene, nthreads: int = 1, flags: Optional[int] = None, light=None
     rgba = np.zeros((scene.height, scene.width, 4), np.uint8)
     z = np.zeros((scene.height, scene.width), np.float32)
     tpf = C.c_int64(0)
+    if face_ids:
+        ids = np.zeros((scene.height, scene.width), np.uint32)
+        st = lib().orc_draw_ids(items, len(scene.objects), C.byref(fr), rgba.ctypes.data, z.ctypes.data,
+                                ids.ctypes.data, C.byref(tpf), nthreads)
+        return rgba, z, int(tpf.value), int(st), ids
     st = lib().orc_draw(items, len(scene.objects), C.byref(fr), rgba.ctypes.data, z.ctypes.data,
                         C.byref(tpf), nthreads)
     return rgba, z, int(tpf.value), int(st)
+
+
+# ---- differentiable shading extension (FP64) ----
+
+def diff_eval(mesh, views, params, ids: np.ndarray, target: np.ndarray, texel_in: Optional[np.ndarray] = None,
+              grads: bool = True, image: bool = False):
+    """FP64 loss (and gradients) of the differentiable shading model.
+
+    mesh: scenes.MeshData (vidx, nidx, vnrm, uv); views: list of (width, height, screen16, mvp16);
+    params: dict with pos (nv x 4), vcol (nv x 3), tex (th x tw x 4 or None), light (3), world (16),
+    any float dtype (converted to float64); ids, target: per pixel over all views.
+    Returns dict(loss, texel, image?, g_pos, g_vcol, g_tex, g_light)."""
+    keep = []
+
+    def d64(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.asarray(a, np.float64))
+        keep.append(a)
+        return a
+
+    def i32(a):
+        a = np.ascontiguousarray(np.asarray(a, np.int32))
+        keep.append(a)
+        return a
+
+    s = DiffScene()
+    pos, vcol = d64(params["pos"]), d64(params["vcol"])
+    tex = d64(params.get("tex"))
+    s.nv = pos.shape[0]
+    s.nf = mesh.vidx.shape[0]
+    s.nn = mesh.vnrm.shape[0]
+    s.pos, s.vcol = pos.ctypes.data, vcol.ctypes.data
+    s.vidx = i32(mesh.vidx).ctypes.data
+    s.nidx = i32(mesh.nidx).ctypes.data
+    s.vnrm = d64(mesh.vnrm).ctypes.data
+    uv = d64(mesh.uv) if mesh.uv is not None else None
+    s.uv = None if uv is None else uv.ctypes.data
+    s.tex = None if tex is None else tex.ctypes.data
+    s.th, s.tw = (0, 0) if tex is None else (tex.shape[0], tex.shape[1])
+    for k in range(3):
+        s.light[k] = float(params["light"][k])
+    for k in range(16):
+        s.world[k] = float(params["world"][k])
+    vs = (DiffView * len(views))()
+    for i, (w, h, sm, mvp) in enumerate(views):
+        vs[i].width, vs[i].height = w, h
+        for k in range(16):
+            vs[i].screen[k] = float(sm[k])
+            vs[i].mvp[k] = float(mvp[k])
+    npx = sum(w * h for w, h, _, _ in views)
+    ids = np.ascontiguousarray(ids, np.uint32).reshape(-1)
+    target = np.ascontiguousarray(target, np.float32).reshape(-1)
+    assert ids.size == npx and target.size == 4 * npx
+    texel = np.zeros(npx, np.uint32)
+    tin = None if texel_in is None else np.ascontiguousarray(texel_in, np.uint32).reshape(-1)
+    img = np.zeros((npx, 4), np.float64) if image else None
+    out = {}
+    gp = np.zeros((s.nv, 4)) if grads else None
+    gc = np.zeros((s.nv, 3)) if grads else None
+    gt = np.zeros_like(tex) if (grads and tex is not None) else None
+    gl = np.zeros(3) if grads else None
+    out["loss"] = lib().orc_diff_eval(C.byref(s), vs, len(views), ids.ctypes.data, _ptr(tin),
+                                      texel.ctypes.data, target.ctypes.data, _ptr(img), _ptr(gp), _ptr(gc),
+                                      _ptr(gt), _ptr(gl))
+    out["texel"] = texel if tin is None else tin
+    if image:
+        out["image"] = img
+    if grads:
+        out.update(g_pos=gp, g_vcol=gc, g_tex=gt, g_light=gl)
+    return out
