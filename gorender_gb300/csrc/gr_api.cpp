@@ -1348,6 +1348,11 @@ struct gr_diff {
   uint32_t* ids = nullptr;              // per pixel: visible face
   float* z = nullptr;                   // per pixel: zRec of the visible face
   DiffRecord* rec = nullptr;
+  double* vh = nullptr;                 // views x vertices x 3
+  float4* col_tab = nullptr;
+  float4* row_tab = nullptr;
+  uint32_t cols = 0, rows = 0;
+  int max_side = 0;
   float* nhat = nullptr;
   float* d_world = nullptr;
   double* d_acc = nullptr;              // loss, light gradient x 3
@@ -1376,6 +1381,9 @@ DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* targe
   a.nidx = mr.nidx;
   a.uv = mr.uv;
   a.nhat = d->nhat;
+  a.vh = d->vh;
+  a.col_tab = d->col_tab;
+  a.row_tab = d->row_tab;
   a.ids = d->ids;
   a.rec = d->rec;
   a.target = target;
@@ -1387,6 +1395,7 @@ DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* targe
 void diff_free(gr_diff* d) {
   dev_free(d->d_views); dev_free(d->d_frame_views); dev_free(d->d_items);
   dev_free(d->ids); dev_free(d->z); dev_free(d->rec); dev_free(d->nhat); dev_free(d->d_world);
+  dev_free(d->vh); dev_free(d->col_tab); dev_free(d->row_tab);
   dev_free(d->d_acc);
   if (d->h_acc) cudaFreeHost(d->h_acc);
   d->h_acc = nullptr;
@@ -1445,6 +1454,11 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
     hv.H = dv.height;
     hv.pix_base = (uint32_t)pix;
     hv.face_base = (uint32_t)((uint64_t)v * (uint64_t)mr.nf);
+    hv.col_base = d->cols;
+    hv.row_base = d->rows;
+    d->cols += (uint32_t)dv.width;
+    d->rows += (uint32_t)dv.height;
+    d->max_side = std::max(d->max_side, std::max(dv.width, dv.height));
     // Q = rows 0 and 1 of S * MVP (homogeneous screen x and y) and row 3 of
     // MVP (clip W), in double: products of two floats are exact there
     for (int j = 0; j < 4; ++j) {
@@ -1469,6 +1483,9 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st) st = dev_alloc(&d->z, (size_t)pix);
   if (!st) st = dev_alloc(&d->rec, (size_t)pix);
   if (!st) st = dev_alloc(&d->nhat, (size_t)mr.nn * 4);
+  if (!st) st = dev_alloc(&d->vh, (size_t)num_views * (size_t)mr.nv * 3);
+  if (!st) st = dev_alloc(&d->col_tab, (size_t)d->cols);
+  if (!st) st = dev_alloc(&d->row_tab, (size_t)d->rows);
   if (!st) st = dev_alloc(&d->d_world, (size_t)16);
   if (!st) st = dev_alloc(&d->d_acc, (size_t)4);
   if (!st && cudaMallocHost((void**)&d->h_acc, 4 * sizeof(double)) != cudaSuccess) {
@@ -1534,7 +1551,7 @@ int32_t gr_diff_forward(gr_diff* d, const gr_diff_params* p, const float* target
     if ((st = launch(c, pr.a))) return st;
     CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemsetAsync(d->d_acc, 0, sizeof(double), c->stream));
-    e = launch_diff_forward(a, c->stream);
+    e = launch_diff_forward(a, d->max_side, c->stream);
     if (e) return fail(GR_ERR_CUDA, "diff forward: %s", cudaGetErrorString((cudaError_t)e));
     CK(cudaMemcpyAsync(d->h_acc, d->d_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

@@ -16,9 +16,16 @@
 // needs no perspective divide: with Q = S * MVP,
 //   u_i = (Q_0 - x Q_3) . p_i,  v_i = (Q_1 - y Q_3) . p_i       (= (s_i - pixel) * W_i)
 //   D_0 = u_1 v_2 - u_2 v_1 (and cyclic),  b_i = D_i / (D_0 + D_1 + D_2)
-// in double precision: u and v cancel screen positions of hundreds of pixels
-// down to a few, and on thin faces b amplifies what is left, so float32 leaves
-// relative errors up to ~1e-3 where double leaves ~1e-12.
+// u and v cancel screen positions of hundreds of pixels down to a few, and on
+// thin faces D amplifies what is left, so float32 would leave relative errors
+// up to ~1e-3: hx = Q_0.p, hy = Q_1.p and W = Q_3.p are computed once per
+// (view, vertex) in double, and u, v and D per pixel in double from them.
+// The barycentrics are homogeneous of degree 0 in D, so the clip and the
+// normalisation run in float32 on D's correctly signed values:
+//   l_i = max(s D_i, 0) / sum_j max(s D_j, 0),  s = sign(D_0 + D_1 + D_2).
+// The backward chain runs in float32 from those values and from per-column
+// and per-row tables of Q_0 - x Q_3 and Q_1 - y Q_3 (exact in double, then
+// rounded).
 //   colour                        c   = sum_i l_i c_i               (vertex RGB)
 //   intensity                     I   = sum_i l_i (0.5 + 0.5 nhat_i . L)
 //   texel                         t   = tex[floor(v th) mod th][floor(u tw) mod tw],  (u,v) = sum_i l_i uv_i
@@ -130,48 +137,83 @@ __global__ void __launch_bounds__(kThreads) k_diff_normals(const float* __restri
   reinterpret_cast<float4*>(nhat)[n] = make_float4(v.x / len, v.y / len, v.z / len, 0.0f);
 }
 
+// Per (view, vertex): homogeneous screen x and y and clip W, in double.
+__global__ void __launch_bounds__(kThreads) k_diff_vertices(const DiffArgs a) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= a.nv) return;
+  const DiffView& vw = a.views[blockIdx.y];
+  const float4 p = ldg4(a.pos + 4 * (size_t)i);
+  const double x = p.x, y = p.y, z = p.z;
+  double* o = a.vh + 3 * ((size_t)blockIdx.y * (size_t)a.nv + (size_t)i);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const double* q = vw.Q + 4 * r;
+    o[r] = __fma_rn(q[2], z, __fma_rn(q[1], y, __fma_rn(q[0], x, q[3])));
+  }
+}
+
+// Per view: Q_0 - x Q_3 for every column x and Q_1 - y Q_3 for every row y
+// (d u / d p and d v / d p), evaluated in double and rounded to float.
+__global__ void __launch_bounds__(kThreads) k_diff_tables(const DiffArgs a) {
+  const DiffView& vw = a.views[blockIdx.y];
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i < vw.W) {
+    float4 r;
+    r.x = (float)__fma_rn(-(double)i, vw.Q[8], vw.Q[0]);
+    r.y = (float)__fma_rn(-(double)i, vw.Q[9], vw.Q[1]);
+    r.z = (float)__fma_rn(-(double)i, vw.Q[10], vw.Q[2]);
+    r.w = 0.0f;
+    a.col_tab[vw.col_base + i] = r;
+  }
+  if (i < vw.H) {
+    float4 r;
+    r.x = (float)__fma_rn(-(double)i, vw.Q[8], vw.Q[4]);
+    r.y = (float)__fma_rn(-(double)i, vw.Q[9], vw.Q[5]);
+    r.z = (float)__fma_rn(-(double)i, vw.Q[10], vw.Q[6]);
+    r.w = 0.0f;
+    a.row_tab[vw.row_base + i] = r;
+  }
+}
+
 // Geometry of one face at one pixel, shared by the forward and backward passes
 // so that both compute bit-identical values.
 struct FaceGeom {
   int vi[3];
-  double A[3], B[3];  // d u_i / d p_i and d v_i / d p_i (xyz)
-  double u[3], v[3];
-  double D[3], T;     // b_i = D_i / T
+  float u[3], v[3];   // (s_i - pixel) * W_i, rounded from double
+  float d[3];         // s * D_i, rounded from double (s = sign of the sum)
+  float m[3], M;      // max(d_i, 0) and their sum
+  float sg;           // s
   bool ok;
 };
 
-__device__ __forceinline__ double dot4d(const double* q, float4 p) {
-  return __fma_rn(q[3], (double)p.w, __fma_rn(q[2], (double)p.z, __fma_rn(q[1], (double)p.y, q[0] * (double)p.x)));
-}
-
-__device__ __forceinline__ void face_geom(const DiffArgs& a, const DiffView& vw, int f, int px, int py,
-                                          FaceGeom& g) {
+__device__ __forceinline__ void face_geom(const DiffArgs& a, int view, int f, int px, int py, FaceGeom& g) {
   const int* vi = a.vidx + 3 * (size_t)f;
-  double A4[4], B4[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    A4[j] = __fma_rn(-(double)px, vw.Q[8 + j], vw.Q[j]);
-    B4[j] = __fma_rn(-(double)py, vw.Q[8 + j], vw.Q[4 + j]);
-  }
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    g.A[j] = A4[j];
-    g.B[j] = B4[j];
-  }
+  const double X = (double)px, Y = (double)py;
+  double u[3], v[3];
   g.ok = true;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     g.vi[k] = __ldg(vi + k);
-    const float4 p = ldg4(a.pos + 4 * (size_t)g.vi[k]);
-    g.ok = g.ok && dot4d(vw.Q + 8, p) < 0.0;  // W < 0: in front of the camera
-    g.u[k] = dot4d(A4, p);
-    g.v[k] = dot4d(B4, p);
+    const double* h = a.vh + 3 * ((size_t)view * (size_t)a.nv + (size_t)g.vi[k]);
+    const double hx = __ldg(h), hy = __ldg(h + 1), W = __ldg(h + 2);
+    g.ok = g.ok && W < 0.0;  // in front of the camera (W is negative there)
+    u[k] = __fma_rn(-X, W, hx);
+    v[k] = __fma_rn(-Y, W, hy);
+    g.u[k] = (float)u[k];
+    g.v[k] = (float)v[k];
   }
-  g.D[0] = __fma_rn(g.u[1], g.v[2], -(g.u[2] * g.v[1]));
-  g.D[1] = __fma_rn(g.u[2], g.v[0], -(g.u[0] * g.v[2]));
-  g.D[2] = __fma_rn(g.u[0], g.v[1], -(g.u[1] * g.v[0]));
-  g.T = g.D[0] + g.D[1] + g.D[2];
-  g.ok = g.ok && g.T != 0.0 && isfinite(g.T);
+  const double D0 = __fma_rn(u[1], v[2], -(u[2] * v[1]));
+  const double D1 = __fma_rn(u[2], v[0], -(u[0] * v[2]));
+  const double D2 = __fma_rn(u[0], v[1], -(u[1] * v[0]));
+  const double T = D0 + D1 + D2;
+  g.sg = T < 0.0 ? -1.0f : 1.0f;
+  g.d[0] = g.sg * (float)D0;
+  g.d[1] = g.sg * (float)D1;
+  g.d[2] = g.sg * (float)D2;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) g.m[k] = fmaxf(g.d[k], 0.0f);
+  g.M = g.m[0] + g.m[1] + g.m[2];
+  g.ok = g.ok && T != 0.0 && g.M > 0.0f && isfinite(g.M);
 }
 
 struct Shade {
@@ -244,14 +286,11 @@ __global__ void __launch_bounds__(kThreads) k_diff_shade(const DiffArgs a) {
     if (gf != kNoFace) {
       const int f = (int)(gf - vw.face_base);
       FaceGeom g;
-      face_geom(a, vw, f, p % vw.W, p / vw.W, g);
+      face_geom(a, blockIdx.y, f, p % vw.W, p / vw.W, g);
       if (g.ok) {
         // the visibility pass snaps corners to whole pixels, so a pixel may lie
-        // just outside the unsnapped face: clip its barycentrics to the face
-        const double iT = 1.0 / g.T;
-        const double m0 = fmax(g.D[0] * iT, 0.0), m1 = fmax(g.D[1] * iT, 0.0), m2 = fmax(g.D[2] * iT, 0.0);
-        const double ims = 1.0 / (m0 + m1 + m2);
-        const float l0 = (float)(m0 * ims), l1 = (float)(m1 * ims);
+        // just outside the unsnapped face: its barycentrics are clipped to it
+        const float l0 = g.m[0] / g.M, l1 = g.m[1] / g.M;
         uint32_t texel = kNoFace;
         if (a.tex && a.uv) {
           const float l2 = 1.0f - l0 - l1;
@@ -287,8 +326,9 @@ __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
     const DiffRecord rec = a.rec[gp];
     if (rec.face != kNoFace) {
       const int f = (int)(rec.face - vw.face_base);
+      const int px = p % vw.W, py = p / vw.W;
       FaceGeom g;
-      face_geom(a, vw, f, p % vw.W, p / vw.W, g);
+      face_geom(a, blockIdx.y, f, px, py, g);
       const int* ni = a.nidx + 3 * (size_t)f;
       Shade s;
       shade(a, g, rec.l0, rec.l1, rec.texel, ni, s);
@@ -331,33 +371,25 @@ __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
         for (int ch = 0; ch < 3; ++ch) gk += go[ch] * s.I * t3[ch] * s.c[k][ch];
         G[k] = gk;
       }
-      // l_k = m_k / sum m, m_k = max(b_k, 0), b_k = D_k / T (double precision)
-      const double iT = 1.0 / g.T;
-      double b[3], m[3];
+      // l_k = m_k / M, m_k = max(s D_k, 0): d l / d D_j = s [m_j > 0] (G_j - G.l) / M
+      const float Gl = G[0] * s.l[0] + G[1] * s.l[1] + G[2] * s.l[2];
+      float dD[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        b[k] = g.D[k] * iT;
-        m[k] = fmax(b[k], 0.0);
-      }
-      const double ims = 1.0 / (m[0] + m[1] + m[2]);
-      const double Gl = (double)G[0] * (m[0] * ims) + (double)G[1] * (m[1] * ims) + (double)G[2] * (m[2] * ims);
-      double Gb[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) Gb[k] = b[k] > 0.0 ? ((double)G[k] - Gl) * ims : 0.0;
-      const double Gbb = Gb[0] * b[0] + Gb[1] * b[1] + Gb[2] * b[2];
-      double dD[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) dD[k] = (Gb[k] - Gbb) * iT;
+      for (int k = 0; k < 3; ++k) dD[k] = g.m[k] > 0.0f ? g.sg * (G[k] - Gl) / g.M : 0.0f;
       // D_0 = u1 v2 - u2 v1, D_1 = u2 v0 - u0 v2, D_2 = u0 v1 - u1 v0
-      const double gu[3] = {dD[2] * g.v[1] - dD[1] * g.v[2], dD[0] * g.v[2] - dD[2] * g.v[0],
-                            dD[1] * g.v[0] - dD[0] * g.v[1]};
-      const double gv[3] = {dD[1] * g.u[2] - dD[2] * g.u[1], dD[2] * g.u[0] - dD[0] * g.u[2],
-                            dD[0] * g.u[1] - dD[1] * g.u[0]};
+      const float gu[3] = {dD[2] * g.v[1] - dD[1] * g.v[2], dD[0] * g.v[2] - dD[2] * g.v[0],
+                           dD[1] * g.v[0] - dD[0] * g.v[1]};
+      const float gv[3] = {dD[1] * g.u[2] - dD[2] * g.u[1], dD[2] * g.u[0] - dD[0] * g.u[2],
+                           dD[0] * g.u[1] - dD[1] * g.u[0]};
+      // u_k = (Q_0 - x Q_3) . p_k, v_k = (Q_1 - y Q_3) . p_k
+      const float4 A = a.col_tab[vw.col_base + px];
+      const float4 B = a.row_tab[vw.row_base + py];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         float* gp4 = a.g_pos + 4 * (size_t)g.vi[k];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) atomicAdd(gp4 + j, (float)(gu[k] * g.A[j] + gv[k] * g.B[j]));
+        atomicAdd(gp4 + 0, gu[k] * A.x + gv[k] * B.x);
+        atomicAdd(gp4 + 1, gu[k] * A.y + gv[k] * B.y);
+        atomicAdd(gp4 + 2, gu[k] * A.z + gv[k] * B.z);
       }
     }
   }
@@ -382,9 +414,12 @@ int launch_diff_normals(const float* world, const float* vnrm, int nn, float* nh
   return (int)cudaGetLastError();
 }
 
-int launch_diff_forward(const DiffArgs& a, void* stream) {
+int launch_diff_forward(const DiffArgs& a, int max_side, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  k_diff_vertices<<<dim3((unsigned)((a.nv + kThreads - 1) / kThreads), (unsigned)a.num_views), kThreads, 0, s>>>(a);
+  k_diff_tables<<<dim3((unsigned)((max_side + kThreads - 1) / kThreads), (unsigned)a.num_views), kThreads, 0, s>>>(a);
   const dim3 grid((unsigned)((a.max_pixels + kThreads - 1) / kThreads), (unsigned)a.num_views);
-  k_diff_shade<<<grid, kThreads, 0, (cudaStream_t)stream>>>(a);
+  k_diff_shade<<<grid, kThreads, 0, s>>>(a);
   return (int)cudaGetLastError();
 }
 

@@ -173,6 +173,7 @@ struct DiffView {
   int W, H;
   uint32_t pix_base;                // first pixel of this view in the per-pixel buffers
   uint32_t face_base;               // first global face index of this view's item
+  uint32_t col_base, row_base;      // first entry of this view in col_tab / row_tab
 };
 
 // Per-pixel forward record: the visible face (or kNoFace), the texel it
@@ -198,6 +199,9 @@ struct DiffArgs {
   const int* nidx;                  // nf x 3
   const float* uv;                  // nf x 6 (may be null)
   const float* nhat;                // nn x 4: normalised world-space vertex normals
+  double* vh;                       // views x nv x 3: homogeneous screen x, y and clip W
+  float4* col_tab;                  // per view and column x: Q_0 - x Q_3 (xyz)
+  float4* row_tab;                  // per view and row y: Q_1 - y Q_3 (xyz)
   const uint32_t* ids;              // per pixel: global face index or kNoFace (raster output)
   DiffRecord* rec;                  // per pixel
   const float* target;              // per pixel RGBA
@@ -222,7 +226,9 @@ int raster_grid(int tile_shift, int waves);
 int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, void* stream);
 // nhat[n] = xyz of Vec4.Normalize(world * vnrm[n]) (renderer.go:328-331), w = 0.
 int launch_diff_normals(const float* world, const float* vnrm, int nn, float* nhat, void* stream);
-int launch_diff_forward(const DiffArgs& a, void* stream);
+// Per (view, vertex) and per (view, column / row) tables, then per pixel
+// shading; max_side = the largest view width or height.
+int launch_diff_forward(const DiffArgs& a, int max_side, void* stream);
 int launch_diff_backward(const DiffArgs& a, void* stream);
 
 // Records a message for gr_last_error() on this thread and returns code (gr_api.cpp).

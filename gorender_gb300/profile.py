@@ -1,16 +1,21 @@
-"""Renders a named scene for a fixed number of frames (for profilers).
+"""Renders a named workload for a fixed number of iterations (for profilers).
 
-    python -m gorender_gb300.profile --scene heightfield --frames 10
+    python -m gorender_gb300.profile --scene heightfield --frames 10 [--autotune]
 
 Scenes: uvsphere (960 tris, 640x360), heightfield (199,712 tris, 1280x720),
-icospheres (64 level-5/6 icospheres, 1920x1080).  Frames are issued with
-gr_draw_async on the context stream; the process exits non-zero on any error.
+icospheres (64 level-5/6 icospheres, 1920x1080), batch (the 256-view
+multi-view batch, one CUDA-graph replay per iteration) and diff (forward +
+backward of the differentiable icosphere workload, --views views at
+512x512).  Frames are issued with gr_draw_async on the context stream; the
+process exits non-zero on any error.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import time
 
+from . import _native as N
 from . import renderer as R
 from . import scenes
 
@@ -21,15 +26,15 @@ SCENES = {
 }
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--scene", default="heightfield", choices=sorted(SCENES))
-    ap.add_argument("--frames", type=int, default=10)
-    ap.add_argument("--device", type=int, default=0)
-    args = ap.parse_args()
+def run_frames(args):
     sc = SCENES[args.scene]()
     ctx = R.Context(args.device)
     up = R.UploadedScene(ctx, sc)
+    if args.autotune:
+        N.check(N.lib().gr_context_autotune(ctx.handle, up.items, len(sc.objects), C.byref(up.params)))
+    if args.tile or args.slice:
+        ctx.set_tuning(args.tile, 0)
+        N.check(N.lib().gr_context_set_raster(ctx.handle, args.slice, 0))
     up.draw()  # sizes the buffers (and re-runs on overflow)
     t0 = time.perf_counter()
     for _ in range(args.frames):
@@ -37,8 +42,79 @@ def main():
     ctx.sync()
     dt = time.perf_counter() - t0
     print(f"{sc.name}: {args.frames} frames, {dt * 1e3 / args.frames:.4f} ms/frame (host wall clock), "
-          f"{sc.num_triangles * args.frames / dt / 1e6:.1f} Mtris/s")
+          f"{sc.num_triangles * args.frames / dt / 1e6:.1f} Mtris/s, tuning {ctx.tuning()} {ctx.raster()}")
     ctx.close()
+
+
+def run_batch(args):
+    import torch
+
+    vs = scenes.multiview_batch(256, seed=0)
+    ctx = R.Context(args.device)
+    views, entries, keep = [], [], []
+    for v, sc in enumerate(vs):
+        up = R.UploadedScene(ctx, sc)
+        rgba = torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
+        z = torch.empty((sc.height, sc.width), dtype=torch.float32, device="cuda")
+        keep += [rgba, z]
+        views.append((up.params, rgba.data_ptr(), z.data_ptr()))
+        entries += [(h, mvp, w, v) for h, (mvp, w) in zip(up.mesh_handles, up.matrices)]
+    b = R.Batch(ctx, views, entries, autotune=args.autotune)
+    t0 = time.perf_counter()
+    for _ in range(args.frames):
+        b.run()
+    b.sync()
+    dt = time.perf_counter() - t0
+    print(f"batch of {len(vs)} views: {args.frames} replays, {dt * 1e3 / args.frames:.4f} ms/replay, "
+          f"tuning {b.tuning()}")
+    b.close()
+    ctx.close()
+
+
+def run_diff(args):
+    import torch
+
+    sc = scenes.diff_scene(views=args.views, size=512, level=6, tex_size=256, seed=0)
+    ctx = R.Context(args.device)
+
+    def t(a):
+        return torch.as_tensor(a, dtype=torch.float32, device="cuda")
+
+    mesh = ctx.mesh(sc.mesh)
+    world, views = R.diff_views(sc)
+    d = R.Diff(ctx, mesh, world, views, tex_size=sc.tex.shape[:2])
+    npx = sum(w * h for w, h, _, _, _ in views)
+    p = [t(sc.mesh.pos), t(sc.vcol), t(sc.tex)]
+    target = torch.zeros((npx, 4), dtype=torch.float32, device="cuda")
+    g = [torch.empty((sc.mesh.nv, 4), device="cuda"), torch.empty((sc.mesh.nv, 3), device="cuda"),
+         torch.empty(sc.tex.shape, device="cuda")]
+    t0 = time.perf_counter()
+    for _ in range(args.frames):
+        loss = d.forward(p[0].data_ptr(), p[1].data_ptr(), p[2].data_ptr(), sc.light, target.data_ptr())
+        d.backward(*(x.data_ptr() for x in g))
+    dt = time.perf_counter() - t0
+    print(f"diff {args.views} views: {args.frames} forward+backward, {dt * 1e3 / args.frames:.4f} ms each, "
+          f"loss {loss:.6e}")
+    d.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scene", default="heightfield", choices=sorted(SCENES) + ["batch", "diff"])
+    ap.add_argument("--frames", type=int, default=10)
+    ap.add_argument("--views", type=int, default=64, help="views of the diff workload")
+    ap.add_argument("--autotune", action="store_true", help="run the library autotuner first")
+    ap.add_argument("--tile", type=int, default=0, help="raster tile size (16 or 32; 0 keeps the default)")
+    ap.add_argument("--slice", type=int, default=0, help="bin entries per raster slice (0 keeps the default)")
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args()
+    if args.scene == "batch":
+        run_batch(args)
+    elif args.scene == "diff":
+        run_diff(args)
+    else:
+        run_frames(args)
 
 
 if __name__ == "__main__":
