@@ -109,6 +109,10 @@ struct gr_context {
   int views_cap = 0;
   uint2* plan = nullptr;            // raster work queue
   uint32_t plan_cap = 0;
+  Overlay* ovl = nullptr;           // ShowEdges / ShowVertices marks
+  uint32_t ovl_cap = 0;
+  uint32_t* ovl_key = nullptr;      // per pixel of all views (zero when idle)
+  uint64_t ovl_pixels = 0;
   int raster_waves = 1;             // persistent raster CTAs = SMs x resident CTAs x waves
   int last_views = 0;               // views of the last batched draw
   float tuned_ms = 0.0f;            // best batch time seen by the autotuner
@@ -127,7 +131,7 @@ struct gr_context {
   int last_launches = 0;
   int32_t pending = GR_OK;
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes of the last draw
-  uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0, want_clip_cap = 0;
+  uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0, want_clip_cap = 0, want_ovl_cap = 0;
   int tile_shift = kDefaultTileShift;  // raster tile size (autotuned per workload)
 };
 
@@ -354,8 +358,6 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
       return fail(GR_ERR_INVALID_ARGUMENT, "view %d: bad framebuffer size %dx%d", v, p->width, p->height);
     if (p->width > kMaxDim || p->height > kMaxDim)
       return fail(GR_ERR_UNSUPPORTED, "view %d: framebuffer %dx%d exceeds %d", v, p->width, p->height, kMaxDim);
-    if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
-      return fail(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
     if (!views[v].rgba || !views[v].z) return fail(GR_ERR_INVALID_ARGUMENT, "view %d: missing outputs", v);
     const uint64_t t = (uint64_t)((p->width + ts - 1) / ts) * (uint64_t)((p->height + ts - 1) / ts);
     if (total_tiles + t >= (1ull << 31)) return fail(GR_ERR_UNSUPPORTED, "too many raster tiles");
@@ -366,11 +368,22 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   if (st) return st;
   if ((st = upload_textures(c))) return st;
   if ((st = ensure_views(c, nviews, total_tiles))) return st;
+  uint64_t total_pixels = 0;
+  for (int v = 0; v < nviews; ++v) total_pixels += (uint64_t)views[v].p->width * (uint64_t)views[v].p->height;
+  if ((flags_any & (GR_SHOW_EDGES | GR_SHOW_VERTICES)) && total_pixels > c->ovl_pixels) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->ovl_key);
+    c->ovl_pixels = 0;
+    if ((st = dev_alloc(&c->ovl_key, (size_t)total_pixels))) return st;
+    CK(cudaMemsetAsync(c->ovl_key, 0, sizeof(uint32_t) * total_pixels, c->stream));
+    c->ovl_pixels = total_pixels;
+  }
   const int slot = (c->stage_slot + 1) % kStageSlots;
   if (c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
   DevView* hviews = c->h_views + (size_t)slot * c->views_cap;
   DevItem* hitems = c->h_items + (size_t)slot * c->items_cap;
   uint32_t tile_base = 0;
+  uint64_t pix_base = 0;
   for (int v = 0; v < nviews; ++v) {
     const gr_frame_params* p = views[v].p;
     DevView& d = hviews[v];
@@ -386,6 +399,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     for (int k = 0; k < 3; ++k) d.L[k] = p->light[k];
     d.out_rgba = views[v].rgba;
     d.out_z = views[v].z;
+    d.pix_base = pix_base;
+    pix_base += (uint64_t)p->width * (uint64_t)p->height;
     d.vec_ok = (p->width % 4 == 0) && ((uintptr_t)d.out_rgba % 16 == 0) && ((uintptr_t)d.out_z % 16 == 0);
   }
   uint64_t faces = 0;
@@ -429,6 +444,16 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   }
   if (faces >= (1ull << 28)) return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces in one frame");
   if ((st = ensure_frame_buffers(c, faces, total_tiles))) return st;
+  if (flags_any & (GR_SHOW_EDGES | GR_SHOW_VERTICES)) {
+    const uint64_t want_ovl = std::max<uint64_t>(c->want_ovl_cap, std::min<uint64_t>(faces + 1024, 1u << 30));
+    if (want_ovl > c->ovl_cap) {
+      CK(cudaStreamSynchronize(c->stream));
+      dev_free(c->ovl);
+      c->ovl_cap = 0;
+      if ((st = dev_alloc(&c->ovl, want_ovl))) return st;
+      c->ovl_cap = (uint32_t)want_ovl;
+    }
+  }
   if (light_total > c->vlight_cap) {
     CK(cudaStreamSynchronize(c->stream));
     dev_free(c->vlight);
@@ -485,6 +510,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.plan = c->plan;
   a.plan_cap = c->plan_cap;
   a.raster_ctas = raster_grid(c->tile_shift, c->raster_waves);
+  a.ovl = c->ovl;
+  a.ovl_cap = c->ovl_cap;
+  a.ovl_key = c->ovl_key;
   out.faces = faces;
   out.nitems = live;
   return GR_OK;
@@ -506,7 +534,8 @@ uint64_t buffers_signature(const gr_context* c) {
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, c->rec_cap, c->key_cap, c->bin_cap,
                           c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_entries,
-                          (uintptr_t)c->raster_waves, c->texs.size()};
+                          (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key,
+                          c->ovl_cap};
   uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
   for (uintptr_t v : ps) {
     h ^= (uint64_t)v;
@@ -524,7 +553,11 @@ int check_result(gr_context* c, const DevResult& r, int32_t* err) {
   if (r.rec_need > c->rec_cap) { c->want_rec_cap = r.rec_need + r.rec_need / 8; rerun = 1; }
   if (r.big_need > c->big_cap) { c->want_big_cap = next_pow2((uint64_t)r.big_need + r.big_need / 4); rerun = 1; }
   if (r.clip_need > c->clip_cap) { c->want_clip_cap = next_pow2((uint64_t)r.clip_need + r.clip_need / 4); rerun = 1; }
+  if (r.ovl_need > c->ovl_cap) { c->want_ovl_cap = next_pow2((uint64_t)r.ovl_need + r.ovl_need / 4); rerun = 1; }
   if (r.error & 1u) *err = fail(GR_ERR_CLIP_OVERFLOW, "a clipped polygon exceeded 9 vertices");
+  if (r.error & 4u)
+    *err = fail(GR_ERR_UNSUPPORTED, "an edge overlay line has more than %lld steps (a corner far off screen)",
+                (long long)kMaxLineSteps);
   return rerun;
 }
 
@@ -633,6 +666,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
   dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan);
+  dev_free(c->ovl); dev_free(c->ovl_key);
   if (c->h_views) cudaFreeHost(c->h_views);
   if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
   dev_free(c->work); dev_free(c->d_result);

@@ -43,6 +43,7 @@ struct DevView {
   float L[4];                       // light direction (L[3] unused)
   uint32_t* out_rgba;               // H x W RGBA8
   float* out_z;                     // H x W
+  unsigned long long pix_base;      // first pixel of this view in the overlay key buffer
 };
 
 // One draw item in device memory: an Object with its matrices.
@@ -99,6 +100,17 @@ struct TriColor {
   float c[9];
 };
 
+// One binned triangle's overlay marks (ShowEdges / ShowVertices,
+// renderer.go:191-216): its int() corners, its float corners (the centroid
+// mark uses them) and its draw-order key.
+struct Overlay {
+  long long X[3], Y[3];
+  float sx[3], sy[3];
+  uint32_t key;                     // face * 8 + fan + 1
+  uint32_t view;
+};
+constexpr long long kMaxLineSteps = 1ll << 22;  // longer overlay lines are refused (error bit 2)
+
 // Counters the kernels append to.  Zeroed once at allocation; the raster
 // kernel copies them into DevResult and zeroes them again.
 struct DevWork {
@@ -108,17 +120,19 @@ struct DevWork {
   unsigned int bin_need;            // max (bin position + 1) seen when over capacity
   unsigned int rec_need;            // records needed when over capacity
   unsigned int big_need;
-  unsigned int error;               // bit 0 clip overflow, bit 1 bad normal index
+  unsigned int error;               // bit 0 clip overflow, bit 1 bad normal index, bit 2 overlay line too long
   unsigned int nclip;               // faces queued for the general clipper
   unsigned int clip_need;
   unsigned int max_bin;             // largest tile bin of the frame (k_plan)
   unsigned int plan_front, plan_back;  // raster work items: split tiles, whole tiles
   unsigned int raster_next, raster_exit;  // persistent raster: next item, finished CTAs
+  unsigned int novl, ovl_need;      // overlay records written / needed
 };
 
 struct DevResult {
   unsigned long long tpf;           // binned triangles over all views
   unsigned int nrec, nbig, bin_need, rec_need, big_need, error, nclip, clip_need, max_bin, items;
+  unsigned int novl, ovl_need;
 };
 
 // Everything a frame's kernels need, passed by value.
@@ -159,6 +173,9 @@ struct FrameArgs {
   uint2* plan;                      // raster work items (tile, slice), plan_cap entries
   uint32_t plan_cap;
   int raster_ctas;                  // persistent raster grid
+  Overlay* ovl;                     // overlay records (views with ShowEdges / ShowVertices)
+  uint32_t ovl_cap;
+  uint32_t* ovl_key;                // per pixel of every view: max (order key * 2 + vertex mark), 0 = none
 };
 
 // View flag (internal, never set by callers): the raster resolve writes the

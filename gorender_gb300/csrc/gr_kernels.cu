@@ -189,6 +189,33 @@ __device__ __forceinline__ bool bin_test(const SV& a, const SV& b, const SV& c, 
   return maxX >= 0.0f && minX <= Wf && maxY >= 0.0f && minY <= Hf;
 }
 
+// Overlay record of a binned triangle (ShowEdges / ShowVertices).  Called by
+// every lane of a converged warp; one atomic per warp.
+__device__ __forceinline__ void emit_overlay(const FrameArgs& a, bool on, const SV& s0, const SV& s1, const SV& s2,
+                                             uint32_t key, int view) {
+  const unsigned m = __ballot_sync(FULL_MASK, on);
+  if (!m) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int ldr = __ffs(m) - 1;
+  uint32_t b = 0;
+  if ((int)lane == ldr) b = atomicAdd(&a.work->novl, (uint32_t)__popc(m));
+  b = __shfl_sync(FULL_MASK, b, ldr);
+  if (!on) return;
+  const uint32_t q = b + __popc(m & ((1u << lane) - 1u));
+  if (q >= a.ovl_cap) {
+    atomicMax(&a.work->ovl_need, q + 1);
+    return;
+  }
+  Overlay o;
+  o.X[0] = s0.X; o.X[1] = s1.X; o.X[2] = s2.X;
+  o.Y[0] = s0.Y; o.Y[1] = s1.Y; o.Y[2] = s2.Y;
+  o.sx[0] = s0.sx; o.sx[1] = s1.sx; o.sx[2] = s2.sx;
+  o.sy[0] = s0.sy; o.sy[1] = s1.sy; o.sy[2] = s2.sy;
+  o.key = key;
+  o.view = (uint32_t)view;
+  a.ovl[q] = o;
+}
+
 __device__ __forceinline__ long long min3ll(long long a, long long b, long long c) { return min(min(a, b), c); }
 __device__ __forceinline__ long long max3ll(long long a, long long b, long long c) { return max(max(a, b), c); }
 
@@ -548,6 +575,8 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   // TPF: one atomic per warp (all faces of a block belong to one view).
   const int wt = __reduce_add_sync(FULL_MASK, ntpf);
   if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
+  if (fl & 0xC0u)  // ShowEdges / ShowVertices: every binned triangle leaves marks
+    emit_overlay(a, ntpf != 0, s0, s1, s2, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u, it.view);
 
   // Compact records: one atomic per warp, lane offsets from the ballot.
   const unsigned em = __ballot_sync(FULL_MASK, emit);
@@ -735,6 +764,9 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
     }
     const int wt = __reduce_add_sync(FULL_MASK, ntpf);
     if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
+    if (vw.flags & 0xC0u)
+      emit_overlay(a, ntpf != 0, s0, s1, s2,
+                   (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u, it.view);
   }
 }
 
@@ -1178,9 +1210,18 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       const int x = tx0 + col + j;
       const unsigned long long k = keys[j];
       const bool face_ids = vw.flags & kViewFaceIds;
+      // overlay marks (k_overlay): the last mark in draw order, if any
+      uint32_t ov = 0;
+      if ((vw.flags & 0xC0u) && x <= tx1) {
+        uint32_t* op = a.ovl_key + vw.pix_base + (size_t)y * (size_t)vw.W + (size_t)x;
+        ov = *op;
+        if (ov) *op = 0u;  // ready for the next frame
+      }
+      // vertexColor (255,161,0,255); edgeColor black, or white without faces (renderer.go:17-19, 192-196)
+      const uint32_t ovc = (ov & 1u) ? 0xFF00A1FFu : ((vw.flags & 0x02u) ? 0xFF000000u : 0xFFFFFFFFu);
       if (k == BG_KEY || x > tx1) {
         const bool dot = (x % 10 == 0) && (y % 10 == 0) && x >= 10 && y >= 10;  // DotGrid
-        out_c[j] = face_ids ? kNoFace : dot ? 0xFF646464u : 0xFF323232u;
+        out_c[j] = ov ? ovc : face_ids ? kNoFace : dot ? 0xFF646464u : 0xFF323232u;
         out_z[j] = -1.0f;
         continue;
       }
@@ -1215,7 +1256,8 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       } else {
         c = color_intensity(0xFFC8C8C8u, I);  // faceColor (200,200,200,255)
       }
-      out_c[j] = c;
+      // a mark of the winner itself or of a later triangle lies on top of the fill
+      out_c[j] = (ov && (ov >> 1) >= okey) ? ovc : c;
       out_z[j] = z;
     }
     const int x = tx0 + col;
@@ -1231,6 +1273,83 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     }
   }
   if (tid == 0) a.bin_count[tile] = 0;  // ready for the next frame
+}
+
+// ---------------------------------------------------------------------------
+// k_overlay: the marks of ShowEdges / ShowVertices (renderer.go:191-216).
+// They are not depth-tested and overwrite whatever was drawn before them, so
+// a pixel shows the last mark in draw order unless a later triangle's fill
+// (which is necessarily the depth winner: the last fill at a pixel always
+// is) covers it.  Each mark records max(order key * 2 + vertex mark) per
+// pixel; the raster resolve compares it with the winner's key.  One thread
+// per binned triangle: a line's pixels depend on float32 steps accumulated
+// one add at a time (FrameBuffer.Line), so each line runs sequentially.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long go_abs(long long v) {  // utils.go abs: MinInt -> MaxInt
+  if (v < 0) v = (long long)(0ull - (unsigned long long)v);
+  if (v < 0) v = (long long)((unsigned long long)v - 1ull);
+  return v;
+}
+
+// FrameBuffer.Pixel (rasterizer.go:25-30): the linear index decides (an x
+// outside the row wraps into the next), index 0 is never written.
+__device__ __forceinline__ void ovl_plot(const FrameArgs& a, const DevView& vw, long long x, long long y,
+                                         uint32_t val) {
+  typedef unsigned long long u64;
+  const long long idx = (long long)((u64)y * (u64)(long long)vw.W + (u64)x);
+  if (idx > 0 && idx < (long long)vw.W * (long long)vw.H) atomicMax(a.ovl_key + vw.pix_base + (u64)idx, val);
+}
+
+// FrameBuffer.Line (rasterizer.go:65-79)
+__device__ void ovl_line(const FrameArgs& a, const DevView& vw, long long x0, long long y0, long long x1,
+                         long long y1, uint32_t val) {
+  typedef unsigned long long u64;
+  const long long dx = (long long)((u64)x1 - (u64)x0), dy = (long long)((u64)y1 - (u64)y0);
+  const long long side = max(go_abs(dx), go_abs(dy));
+  if (side > kMaxLineSteps) {
+    atomicOr(&a.work->error, 4u);
+    return;
+  }
+  const float xs = fd(__ll2float_rn(dx), __ll2float_rn(side)), ys = fd(__ll2float_rn(dy), __ll2float_rn(side));
+  float cx = __ll2float_rn(x0), cy = __ll2float_rn(y0);
+  for (long long i = 0; i <= side; ++i) {
+    ovl_plot(a, vw, go_int(cx), go_int(cy), val);
+    cx = fa(cx, xs);
+    cy = fa(cy, ys);
+  }
+}
+
+// FrameBuffer.Rect (rasterizer.go:54-63), 3 x 3
+__device__ __forceinline__ void ovl_rect3(const FrameArgs& a, const DevView& vw, long long x, long long y,
+                                          uint32_t val) {
+  if (x >= (long long)vw.W || y >= (long long)vw.H) return;
+  for (int py = 0; py < 3; ++py)
+    for (int px = 0; px < 3; ++px) ovl_plot(a, vw, x + px, y + py, val);
+}
+
+__global__ void __launch_bounds__(256) k_overlay(const FrameArgs a) {
+  const uint32_t n = min(*(volatile uint32_t*)&a.work->novl, a.ovl_cap);
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const Overlay o = a.ovl[q];
+    const DevView& vw = a.views[o.view];
+    const uint32_t fl = vw.flags;
+    const uint32_t edge = o.key * 2u, vert = o.key * 2u + 1u;  // vertex marks come after the edges
+    if (fl & 0x40u) {
+      ovl_line(a, vw, o.X[0], o.Y[0], o.X[1], o.Y[1], edge);
+      ovl_line(a, vw, o.X[1], o.Y[1], o.X[2], o.Y[2], edge);
+      ovl_line(a, vw, o.X[2], o.Y[2], o.X[0], o.Y[0], edge);
+      if (fl & 0x02u) {
+        const float cx = fd(fa(fa(o.sx[0], o.sx[1]), o.sx[2]), 3.0f);
+        const float cy = fd(fa(fa(o.sy[0], o.sy[1]), o.sy[2]), 3.0f);
+        ovl_rect3(a, vw, (long long)((unsigned long long)go_int(cx) - 1ull),
+                  (long long)((unsigned long long)go_int(cy) - 1ull), edge);
+      }
+    }
+    if (fl & 0x80u)
+      for (int j = 0; j < 3; ++j)
+        ovl_rect3(a, vw, (long long)((unsigned long long)o.X[j] - 1ull), (long long)((unsigned long long)o.Y[j] - 1ull),
+                  vert);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1323,6 +1442,9 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     r->clip_need = w->clip_need;
     r->max_bin = w->max_bin;
     r->items = total;
+    r->novl = w->novl;
+    r->ovl_need = w->ovl_need;
+    w->novl = 0; w->ovl_need = 0;
     w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
     w->nclip = 0; w->clip_need = 0; w->max_bin = 0;
     w->plan_front = 0; w->plan_back = 0; w->raster_next = 0; w->raster_exit = 0;
@@ -1365,6 +1487,10 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     }
     k_bin_big<<<big_blocks, 256, 0, s>>>(a);
     ++n;
+    if (a.flags_any & 0xC0u) {
+      k_overlay<<<big_blocks, 256, 0, s>>>(a);
+      ++n;
+    }
     if (events) cudaEventRecord((cudaEvent_t)events[2], s);
   } else if (events) {
     cudaEventRecord((cudaEvent_t)events[1], s);

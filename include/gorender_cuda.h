@@ -39,7 +39,8 @@ extern "C" {
 #define GR_ERR_CLIP_OVERFLOW 6    /* a clipped polygon exceeded 9 vertices
                                      (the reference panics here) */
 #define GR_ERR_NO_DEVICE 7
-#define GR_ERR_UNSUPPORTED 8      /* e.g. framebuffer larger than 16384 x 16384 */
+#define GR_ERR_UNSUPPORTED 8      /* e.g. framebuffer larger than 16384 x 16384, or an edge
+                                     overlay line of more than 2^22 steps */
 
 /* ---- Renderer flags (renderer.go:90-98); defaults of NewRenderer are
  *      GR_FLAGS_DEFAULT (renderer.go:130-148). ---- */
@@ -49,8 +50,8 @@ extern "C" {
 #define GR_LIGHTING 0x08u
 #define GR_FLAT_SHADING 0x10u
 #define GR_SHOW_TEXTURES 0x20u
-#define GR_SHOW_EDGES 0x40u    /* overlay not implemented: rejected with GR_ERR_UNSUPPORTED */
-#define GR_SHOW_VERTICES 0x80u /* overlay not implemented: rejected with GR_ERR_UNSUPPORTED */
+#define GR_SHOW_EDGES 0x40u    /* edge lines + centroid marks, drawn in draw order (renderer.go:191-209) */
+#define GR_SHOW_VERTICES 0x80u /* vertex marks (renderer.go:212-216); both overlays: not in gr_draw_noalloc */
 #define GR_FLAGS_DEFAULT (GR_FRUSTUM_CLIPPING | GR_SHOW_FACES | GR_BACKFACE_CULLING | GR_LIGHTING | GR_SHOW_TEXTURES)
 
 /* ---- texture kinds (texture.go:12-17) ---- */

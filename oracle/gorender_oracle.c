@@ -437,6 +437,7 @@ typedef struct {
   int32_t tex;      /* -1 = nil */
   int32_t has_col;  /* per-vertex RGB extension active */
   uint32_t face;    /* global face index: earlier objects' faces + face index */
+  float sx[3], sy[3];  /* screen coordinates before int() (the centroid mark uses them) */
 } RTri;
 
 /* FrameBuffer.Triangle (rasterizer.go:90-183) restricted to rows
@@ -671,6 +672,7 @@ static int project_object(const orc_item* it, const orc_frame* fr, uint32_t face
       t.tex = tex;
       t.has_col = m->vcolor != NULL;
       t.face = face_base + (uint32_t)fi;
+      for (int j = 0; j < 3; j++) { t.sx[j] = sp[j].x; t.sy[j] = sp[j].y; }
       int e = tl_push(out, &t);
       if (e) return e;
     }
@@ -694,23 +696,113 @@ typedef struct {
   float* z;
   uint32_t* ids;          /* optional: face that wrote each pixel */
   uint32_t* face_base;    /* per item */
+  int band_err;           /* overlay error seen by a raster band */
   int32_t nthreads;
   int32_t band;           /* band index for the raster phase */
 } DrawCtx;
 
+/* ---- overlays: ShowEdges / ShowVertices (renderer.go:191-216) ---- */
+
+static const uint8_t kEdgeColor[4] = {0, 0, 0, 255};        /* renderer.go:19 */
+static const uint8_t kVertexColor[4] = {255, 161, 0, 255};  /* renderer.go:18 */
+static const uint8_t kWhite[4] = {255, 255, 255, 255};      /* renderer.go:195 */
+
+typedef struct {
+  uint8_t* rgba;
+  int64_t width, npx;
+  int64_t y0, y1;          /* band: rows of the linear index that this pass owns */
+  int err;
+} Plot;
+
+/* FrameBuffer.Pixel (rasterizer.go:25-30): the linear index decides, so an
+ * x outside [0, width) wraps into a neighbouring row, and index 0 is never
+ * written. */
+static void plot(Plot* p, int64_t x, int64_t y, const uint8_t* c) {
+  const int64_t idx = wadd(wmul(y, p->width), x);
+  if (!(idx > 0 && idx < p->npx)) return;
+  const int64_t row = idx / p->width;
+  if (row < p->y0 || row >= p->y1) return;
+  memcpy(p->rgba + 4 * idx, c, 4);
+}
+
+/* utils.go abs: MinInt maps to MaxInt */
+static int64_t go_abs(int64_t v) {
+  if (v < 0) v = (int64_t)(0 - (uint64_t)v);
+  if (v < 0) v = (int64_t)((uint64_t)v - 1);
+  return v;
+}
+
+/* FrameBuffer.Line (rasterizer.go:65-79): DDA with float32 steps accumulated
+ * one add at a time.  Lines of more than ORC_MAX_LINE_STEPS steps are refused
+ * (error -6): the reference would plot them for a very long time. */
+#define ORC_MAX_LINE_STEPS (1ll << 22)
+static void draw_line(Plot* p, int64_t x0, int64_t y0, int64_t x1, int64_t y1, const uint8_t* c) {
+  const int64_t dx = wsub(x1, x0), dy = wsub(y1, y0);
+  const int64_t ax = go_abs(dx), ay = go_abs(dy);
+  const int64_t side = ax > ay ? ax : ay;
+  if (side > ORC_MAX_LINE_STEPS) { p->err = -6; return; }
+  const float xs = (float)dx / (float)side, ys = (float)dy / (float)side;
+  float cx = (float)x0, cy = (float)y0;
+  for (int64_t i = 0; i <= side; i++) {
+    plot(p, orc_go_int(cx), orc_go_int(cy), c);
+    cx += xs;
+    cy += ys;
+  }
+}
+
+/* FrameBuffer.Rect (rasterizer.go:54-63) */
+static void draw_rect(Plot* p, int64_t x, int64_t y, int64_t w, int64_t h, const uint8_t* c) {
+  if (x >= p->width || y >= p->npx / p->width) return;
+  for (int64_t py = y; py < wadd(y, h); py++)
+    for (int64_t px = x; px < wadd(x, w); px++) plot(p, px, py, c);
+}
+
+int orc_fb_line(uint8_t* rgba, int32_t width, int32_t height, int64_t x0, int64_t y0, int64_t x1, int64_t y1,
+                const uint8_t* color) {
+  Plot p = {rgba, width, (int64_t)width * height, 0, height, 0};
+  draw_line(&p, x0, y0, x1, y1, color);
+  return p.err;
+}
+
+void orc_fb_rect(uint8_t* rgba, int32_t width, int32_t height, int64_t x, int64_t y, int64_t w, int64_t h,
+                 const uint8_t* color) {
+  Plot p = {rgba, width, (int64_t)width * height, 0, height, 0};
+  draw_rect(&p, x, y, w, h, color);
+}
+
+static void overlays(Plot* p, const RTri* t, uint32_t fl) {
+  if (fl & ORC_SHOW_EDGES) {
+    const uint8_t* col = (fl & ORC_SHOW_FACES) ? kEdgeColor : kWhite;
+    draw_line(p, t->x[0], t->y[0], t->x[1], t->y[1], col);
+    draw_line(p, t->x[1], t->y[1], t->x[2], t->y[2], col);
+    draw_line(p, t->x[2], t->y[2], t->x[0], t->y[0], col);
+    if (fl & ORC_SHOW_FACES) {
+      const float cx = (t->sx[0] + t->sx[1] + t->sx[2]) / 3;
+      const float cy = (t->sy[0] + t->sy[1] + t->sy[2]) / 3;
+      draw_rect(p, wsub(orc_go_int(cx), 1), wsub(orc_go_int(cy), 1), 3, 3, col);
+    }
+  }
+  if (fl & ORC_SHOW_VERTICES)
+    for (int j = 0; j < 3; j++) draw_rect(p, wsub(t->x[j], 1), wsub(t->y[j], 1), 3, 3, kVertexColor);
+}
+
 static void raster_band(DrawCtx* c, int64_t y0, int64_t y1) {
   const orc_frame* fr = c->fr;
   const uint32_t fl = fr->flags;
-  if (!(fl & ORC_SHOW_FACES)) return;
+  Plot pl = {c->rgba, fr->width, (int64_t)fr->width * fr->height, y0, y1, 0};
   for (int32_t i = 0; i < c->nitems; i++) {
     const TriList* l = &c->lists[i];
     for (int64_t k = 0; k < l->n; k++) {
       const RTri* t = &l->v[k];
-      const orc_texture* tx = NULL;
-      if ((fl & ORC_SHOW_TEXTURES) && t->tex >= 0) tx = &fr->textures[t->tex];  /* renderer.go:176-178 */
-      raster_tri(c->rgba, c->z, c->ids, fr->width, fr->height, t, 0, 0, fr->width, fr->height, tx, y0, y1);
+      if (fl & ORC_SHOW_FACES) {
+        const orc_texture* tx = NULL;
+        if ((fl & ORC_SHOW_TEXTURES) && t->tex >= 0) tx = &fr->textures[t->tex];  /* renderer.go:176-178 */
+        raster_tri(c->rgba, c->z, c->ids, fr->width, fr->height, t, 0, 0, fr->width, fr->height, tx, y0, y1);
+      }
+      if (fl & (ORC_SHOW_EDGES | ORC_SHOW_VERTICES)) overlays(&pl, t, fl);
     }
   }
+  if (pl.err) __atomic_store_n(&c->band_err, pl.err, __ATOMIC_RELAXED);
 }
 
 static void* project_worker(void* arg) {
@@ -822,6 +914,7 @@ int orc_draw_ids(const orc_item* items, int32_t nitems, const orc_frame* fr, uin
       }
       for (int k = 0; k < nt; k++) pthread_join(th[k], NULL);
     }
+    if (c.band_err) err = c.band_err;
   }
   for (int32_t i = 0; i < nitems; i++) free(c.lists[i].v);
   free(c.lists);

@@ -89,7 +89,10 @@ typedef struct {
  * projects objects concurrently and rasterises in disjoint horizontal bands,
  * which yields the same bytes as nthreads == 1.  Returns 0, or a negative
  * error: -1 bad vertex index, -2 bad normal index, -3 clip polygon overflow,
- * -4 out of memory, -5 bad texture slot. */
+ * -4 out of memory, -5 bad texture slot, -6 an overlay line of more than
+ * 2^22 steps (ShowEdges on a triangle with far-away corners).  ShowEdges
+ * and ShowVertices draw the reference's overlays in draw order
+ * (renderer.go:191-216, FrameBuffer.Line/Rect/Pixel). */
 int orc_draw(const orc_item* items, int32_t nitems, const orc_frame* fr,
              uint8_t* rgba, float* z, int64_t* tpf, int32_t nthreads);
 
@@ -170,6 +173,13 @@ void orc_fb_triangle(uint8_t* rgba, float* z, int32_t width, int32_t height,
                      int64_t x2, int64_t y2, float z2, float u2, float v2,
                      int64_t tsx, int64_t tsy, int64_t tex_, int64_t tey,
                      float ia, float ib, float ic, const orc_texture* texture);
+/* FrameBuffer.Line (rasterizer.go:65-79) and FrameBuffer.Rect (54-63) on an
+ * existing buffer; both plot through FrameBuffer.Pixel (25-30).  orc_fb_line
+ * returns -6 (and draws nothing) for more than 2^22 steps. */
+int orc_fb_line(uint8_t* rgba, int32_t width, int32_t height, int64_t x0, int64_t y0, int64_t x1, int64_t y1,
+                const uint8_t* color);
+void orc_fb_rect(uint8_t* rgba, int32_t width, int32_t height, int64_t x, int64_t y, int64_t w, int64_t h,
+                 const uint8_t* color);
 /* NewMesh face normals (mesh.go:53-60) and boundingBox (mesh.go:28-51). */
 void orc_mesh_face_normals(const float* pos, const int32_t* vidx, int32_t nf,
                            float* fnrm_out);

@@ -107,6 +107,11 @@ def lib():
                                       C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float,
                                       C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                       C.c_float, C.c_float, C.c_float, C.POINTER(Texture)]
+        L.orc_fb_line.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                  C.c_void_p]
+        L.orc_fb_line.restype = C.c_int
+        L.orc_fb_rect.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                  C.c_void_p]
         L.orc_mesh_face_normals.argtypes = [fp, C.c_void_p, C.c_int32, fp]
         L.orc_mesh_bbox.argtypes = [fp, C.c_int32, fp]
         L.orc_world_matrix.argtypes = [fp, fp, fp, fp]

@@ -41,10 +41,24 @@ def inside_sphere():
                             scenes.DEFAULT_FLAGS & ~scenes.BACKFACE_CULLING)
 
 
+def overlays_uvsphere():
+    sc = scenes.scene_uvsphere_640x360()
+    return dataclasses.replace(sc, name="overlays", width=320, height=180,
+                               flags=sc.flags | scenes.SHOW_EDGES | scenes.SHOW_VERTICES)
+
+
+def overlays_wire_heightfield():
+    # ShowFaces off: white edges only, no fills, no centroid marks
+    sc = heightfield_small()
+    return dataclasses.replace(sc, name="wire", flags=(sc.flags | scenes.SHOW_EDGES) & ~scenes.SHOW_FACES)
+
+
 GOLDEN_SCENES = {
     "uvsphere960-640x360": uvsphere,
     "heightfield97-320x180": heightfield_small,
     "icospheres6-320x240": icospheres_small,
     "textures-mixed-160x120": textures_mixed,
     "inside-sphere-160x120": inside_sphere,
+    "overlays-uvsphere-320x180": overlays_uvsphere,
+    "wire-heightfield97-320x180": overlays_wire_heightfield,
 }
