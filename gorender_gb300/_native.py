@@ -19,6 +19,7 @@ GR_ERR_BIN_OVERFLOW = 5
 GR_ERR_CLIP_OVERFLOW = 6
 GR_ERR_NO_DEVICE = 7
 GR_ERR_UNSUPPORTED = 8
+GR_CROSSHAIR = 0x100
 
 STATUS_NAMES = {0: "GR_OK", 1: "GR_ERR_INVALID_ARGUMENT", 2: "GR_ERR_CUDA", 3: "GR_ERR_OUT_OF_MEMORY",
                 4: "GR_ERR_BAD_INDEX", 5: "GR_ERR_BIN_OVERFLOW", 6: "GR_ERR_CLIP_OVERFLOW",
@@ -37,7 +38,7 @@ EXPORTS = [
     "gr_draw_views", "gr_context_view_tpf", "gr_batch_create", "gr_batch_run", "gr_batch_sync",
     "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_get_raster",
     "gr_context_autotune", "gr_diff_create", "gr_diff_forward", "gr_diff_backward", "gr_diff_buffers",
-    "gr_diff_destroy",
+    "gr_diff_destroy", "gr_fog", "gr_context_set_fog", "gr_renderer_fog",
 ]
 
 
@@ -170,6 +171,9 @@ def lib() -> C.CDLL:
             "gr_diff_backward": [vp, C.POINTER(DiffGrads)],
             "gr_diff_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int64)],
             "gr_diff_destroy": [vp],
+            "gr_fog": [vp, vp, vp, i32, i32, C.c_float, C.c_float, vp],
+            "gr_context_set_fog": [vp, i32, C.c_float, C.c_float, vp],
+            "gr_renderer_fog": [vp, C.c_float, C.c_float, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)

@@ -109,6 +109,9 @@ struct gr_context {
   int views_cap = 0;
   uint2* plan = nullptr;            // raster work queue
   uint32_t plan_cap = 0;
+  bool fog_on = false;              // FrameBuffer.Fog fused into every frame
+  float fog_start = 0.0f, fog_end = 0.0f;
+  uint32_t fog_color = 0;
   Overlay* ovl = nullptr;           // ShowEdges / ShowVertices marks
   uint32_t ovl_cap = 0;
   uint32_t* ovl_key = nullptr;      // per pixel of all views (zero when idle)
@@ -310,6 +313,7 @@ struct ViewIn {
   const gr_frame_params* p;
   uint32_t* rgba;
   float* z;
+  bool internal = false;  // may carry library-internal view flags (kViewFaceIds)
 };
 
 int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
@@ -359,6 +363,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     if (p->width > kMaxDim || p->height > kMaxDim)
       return fail(GR_ERR_UNSUPPORTED, "view %d: framebuffer %dx%d exceeds %d", v, p->width, p->height, kMaxDim);
     if (!views[v].rgba || !views[v].z) return fail(GR_ERR_INVALID_ARGUMENT, "view %d: missing outputs", v);
+    if (p->flags & ~(0x1FFu | (views[v].internal ? kViewFaceIds : 0u)))
+      return fail(GR_ERR_INVALID_ARGUMENT, "view %d: unknown flag bits 0x%x", v, p->flags & ~0x1FFu);
     const uint64_t t = (uint64_t)((p->width + ts - 1) / ts) * (uint64_t)((p->height + ts - 1) / ts);
     if (total_tiles + t >= (1ull << 31)) return fail(GR_ERR_UNSUPPORTED, "too many raster tiles");
     total_tiles += (uint32_t)t;
@@ -401,6 +407,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     d.out_z = views[v].z;
     d.pix_base = pix_base;
     pix_base += (uint64_t)p->width * (uint64_t)p->height;
+    d.fog_on = c->fog_on && !(p->flags & kViewFaceIds);
+    d.fog_start = c->fog_start;
+    d.fog_end = c->fog_end;
+    d.fog_color = c->fog_color;
     d.vec_ok = (p->width % 4 == 0) && ((uintptr_t)d.out_rgba % 16 == 0) && ((uintptr_t)d.out_z % 16 == 0);
   }
   uint64_t faces = 0;
@@ -1257,6 +1267,11 @@ int32_t gr_renderer_tpf(gr_renderer* r, int64_t* tpf) {
   return GR_OK;
 }
 
+int32_t gr_renderer_fog(gr_renderer* r, float fog_start, float fog_end, const uint8_t* color4) {
+  if (!r || !color4) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  return gr_fog(r->ctx, (uint8_t*)r->rgba, r->z, r->width, r->height, fog_start, fog_end, color4);
+}
+
 // ---- timing helpers ----
 
 int32_t gr_context_event_record(gr_context* c, int32_t slot) {
@@ -1529,7 +1544,7 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st) {
     d->vin.resize(num_views);
     for (int v = 0; v < num_views; ++v)
-      d->vin[v] = ViewIn{&d->params[v], d->ids + d->hviews[v].pix_base, d->z + d->hviews[v].pix_base};
+      d->vin[v] = ViewIn{&d->params[v], d->ids + d->hviews[v].pix_base, d->z + d->hviews[v].pix_base, true};
     cudaError_t e = cudaMemcpyAsync(d->d_views, d->hviews.data(), sizeof(DiffView) * num_views,
                                     cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess)
@@ -1645,6 +1660,34 @@ int32_t gr_diff_destroy(gr_diff* d) {
     diff_free(d);
   }
   delete d;
+  return GR_OK;
+}
+
+
+int32_t gr_fog(gr_context* c, uint8_t* rgba_dev, const float* z_dev, int32_t width, int32_t height,
+               float fog_start, float fog_end, const uint8_t* color4) {
+  if (!c || !rgba_dev || !z_dev || !color4) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (width <= 0 || height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
+  if (!is_device_ptr(rgba_dev) || !is_device_ptr(z_dev))
+    return fail(GR_ERR_INVALID_ARGUMENT, "gr_fog needs device buffers");
+  if ((uintptr_t)rgba_dev % 4) return fail(GR_ERR_INVALID_ARGUMENT, "rgba needs 4-byte alignment");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  uint32_t col;
+  std::memcpy(&col, color4, 4);
+  const int e = launch_fog((uint32_t*)rgba_dev, z_dev, (long long)width * height, fog_start, fog_end, col, c->stream);
+  if (e) return fail(GR_ERR_CUDA, "fog: %s", cudaGetErrorString((cudaError_t)e));
+  CK(cudaStreamSynchronize(c->stream));
+  return GR_OK;
+}
+
+int32_t gr_context_set_fog(gr_context* c, int32_t enable, float fog_start, float fog_end, const uint8_t* color4) {
+  if (!c || (enable && !color4)) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->fog_on = enable != 0;
+  c->fog_start = fog_start;
+  c->fog_end = fog_end;
+  if (enable) std::memcpy(&c->fog_color, color4, 4);
   return GR_OK;
 }
 

@@ -44,6 +44,9 @@ struct DevView {
   uint32_t* out_rgba;               // H x W RGBA8
   float* out_z;                     // H x W
   unsigned long long pix_base;      // first pixel of this view in the overlay key buffer
+  int fog_on;                       // FrameBuffer.Fog after the frame
+  float fog_start, fog_end;
+  uint32_t fog_color;               // RGBA little-endian
 };
 
 // One draw item in device memory: an Object with its matrices.
@@ -229,6 +232,10 @@ struct DiffArgs {
   float* g_tex;                     // th x tw x 4
   double* g_light;                  // 3, accumulated
 };
+
+// FrameBuffer.Fog on one framebuffer (gr_kernels.cu).
+int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start, float fog_end, uint32_t color,
+               void* stream);
 
 // Kernel launchers (gr_kernels.cu).
 // events (optional): 4 cudaEvent_t recorded before k_project, after k_project,

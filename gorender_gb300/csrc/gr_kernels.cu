@@ -25,6 +25,8 @@
 // that triangle's own zRec bits.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "gr_internal.h"
 
 namespace gr {
@@ -835,6 +837,52 @@ __device__ __forceinline__ uint32_t color_intensity(uint32_t c, float I) {
   return r | (g << 8) | (b << 16) | (c & 0xFF000000u);
 }
 
+// FrameBuffer.CrossHair (rasterizer.go:209-217): four 3-pixel lines 3..5
+// pixels from the centre, plotted through FrameBuffer.Pixel (linear index,
+// index 0 skipped).  True when pixel (x, y) is one of them.
+__device__ __forceinline__ bool crosshair_hit(int W, int H, int x, int y) {
+  const long long cx = W / 2, cy = H / 2, i = (long long)y * W + x, n = (long long)W * H;
+#pragma unroll
+  for (int k = 3; k <= 5; ++k) {
+    const long long p[4] = {cy * W + (cx - k), cy * W + (cx + k), (cy - k) * W + cx, (cy + k) * W + cx};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (p[q] == i && p[q] > 0 && p[q] < n) return true;
+  }
+  return false;
+}
+
+// FrameBuffer.Fog for one pixel (rasterizer.go:193-207) with blendRGBA
+// (185-191): uint8(float32(a)*(1-f) + float32(b)*f) per channel.
+__device__ __forceinline__ uint32_t fog_pixel(uint32_t c, float depth, float fog_start, float fog_end,
+                                              uint32_t fog_color) {
+  if (depth >= fog_start) return c;
+  if (depth <= fog_end) return fog_color;
+  const float f = fs(1.0f, fd(fs(fog_end, depth), fs(fog_end, fog_start)));
+  const float g = fs(1.0f, f);
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float a = (float)((c >> (8 * k)) & 0xFFu), b = (float)((fog_color >> (8 * k)) & 0xFFu);
+    r |= go_u8(fa(fm(a, g), fm(b, f))) << (8 * k);
+  }
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_fog(uint32_t* rgba, const float* z, long long n, float fog_start,
+                                             float fog_end, uint32_t color) {
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (long long)gridDim.x * 256)
+    rgba[i] = fog_pixel(rgba[i], z[i], fog_start, fog_end, color);
+}
+
+int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start, float fog_end, uint32_t color,
+               void* stream) {
+  if (pixels <= 0) return 0;
+  const long long blocks = std::min<long long>((pixels + 255) / 256, 152ll * 16);
+  k_fog<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(rgba, z, pixels, fog_start, fog_end, color);
+  return (int)cudaGetLastError();
+}
+
 // Edge values of record t at pixel (x, y).
 __device__ __forceinline__ void edges_at(const TriRaster& t, const TriWide* wide, uint32_t r, int x, int y,
                                          bool& inside, float& e12f, float& e20f) {
@@ -1260,6 +1308,15 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       out_c[j] = (ov && (ov >> 1) >= okey) ? ovc : c;
       out_z[j] = z;
     }
+    if (vw.flags & (0x100u | kViewFaceIds)) {
+      if (!(vw.flags & kViewFaceIds))
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (crosshair_hit(vw.W, vw.H, tx0 + col + j, y)) out_c[j] = 0xFF00FFFFu;  // (255,255,0,255)
+    }
+    if (vw.fog_on && !(vw.flags & kViewFaceIds))
+#pragma unroll
+      for (int j = 0; j < 4; ++j) out_c[j] = fog_pixel(out_c[j], out_z[j], vw.fog_start, vw.fog_end, vw.fog_color);
     const int x = tx0 + col;
     const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
     if (vw.vec_ok && x + 3 <= tx1) {

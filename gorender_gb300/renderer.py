@@ -26,6 +26,7 @@ FLAT_SHADING = 0x10
 SHOW_TEXTURES = 0x20
 SHOW_EDGES = 0x40
 SHOW_VERTICES = 0x80
+CROSSHAIR = 0x100  # FrameBuffer.CrossHair after the scene (the reference's demoMode off)
 FLAGS_DEFAULT = FRUSTUM_CLIPPING | SHOW_FACES | BACKFACE_CULLING | LIGHTING | SHOW_TEXTURES
 
 
@@ -182,6 +183,17 @@ class Context:
     def flush_l2(self, nbytes: int = 512 << 20):
         N.check(N.lib().gr_context_flush_l2(self._h, nbytes))
 
+    def set_fog(self, enable: bool, fog_start: float = 0.0, fog_end: float = 0.0, color=(0, 0, 0, 0)):
+        """Fog fused into every later frame (gr_context_set_fog)."""
+        col = (C.c_uint8 * 4)(*color)
+        N.check(N.lib().gr_context_set_fog(self._h, 1 if enable else 0, fog_start, fog_end, C.cast(col, C.c_void_p)))
+
+    def fog(self, rgba_dev: int, z_dev: int, width: int, height: int, fog_start: float, fog_end: float, color):
+        """FrameBuffer.Fog on a device framebuffer (gr_fog)."""
+        col = (C.c_uint8 * 4)(*color)
+        N.check(N.lib().gr_fog(self._h, int(rgba_dev), int(z_dev), width, height, fog_start, fog_end,
+                               C.cast(col, C.c_void_p)))
+
     def set_tuning(self, tile_size: int = 0, bin_capacity: int = 0):
         N.check(N.lib().gr_context_set_tuning(self._h, tile_size, bin_capacity))
 
@@ -335,6 +347,11 @@ class Renderer:
         out = np.empty((self.height, self.width), np.float32)
         N.check(N.lib().gr_renderer_read(self._h, None, out.ctypes.data))
         return out
+
+    def fog(self, fog_start: float, fog_end: float, color) -> None:
+        """FrameBuffer.Fog (rasterizer.go:193-207) on the last frame."""
+        col = (C.c_uint8 * 4)(*color)
+        N.check(N.lib().gr_renderer_fog(self._h, fog_start, fog_end, C.cast(col, C.c_void_p)))
 
     def close(self):
         if self._h:

@@ -53,6 +53,10 @@ extern "C" {
 #define GR_SHOW_EDGES 0x40u    /* edge lines + centroid marks, drawn in draw order (renderer.go:191-209) */
 #define GR_SHOW_VERTICES 0x80u /* vertex marks (renderer.go:212-216); both overlays: not in gr_draw_noalloc */
 #define GR_FLAGS_DEFAULT (GR_FRUSTUM_CLIPPING | GR_SHOW_FACES | GR_BACKFACE_CULLING | GR_LIGHTING | GR_SHOW_TEXTURES)
+/* Not a Renderer field: FrameBuffer.CrossHair (rasterizer.go:209-217) after
+ * the scene, as Draw does when the reference's demoMode constant is false
+ * (renderer.go:476-478; the reference ships with demoMode = true). */
+#define GR_CROSSHAIR 0x100u
 
 /* ---- texture kinds (texture.go:12-17) ---- */
 #define GR_TEXTURE_SOLID 0
@@ -212,6 +216,22 @@ int32_t gr_renderer_draw(gr_renderer* r, const gr_object* objects, int32_t num_o
  * memory (either pointer may be NULL). */
 int32_t gr_renderer_read(gr_renderer* r, uint8_t* rgba_out, float* z_out);
 int32_t gr_renderer_tpf(gr_renderer* r, int64_t* tpf);
+/* FrameBuffer.Fog (rasterizer.go:193-207) on the renderer's last frame. */
+int32_t gr_renderer_fog(gr_renderer* r, float fog_start, float fog_end, const uint8_t* color4);
+
+/* ---- fog (rasterizer.go:185-207) ----
+ * FrameBuffer.Fog: pixels with depth >= fog_start keep their colour, those
+ * with depth <= fog_end take color4, the rest blend by
+ * f = 1 - (fog_end - depth) / (fog_end - fog_start) (blendRGBA, alpha too).
+ * The reference's Draw does not call it (renderer.go:479 is commented out). */
+/* On any framebuffer in device memory (RGBA8 + Z of width x height). */
+int32_t gr_fog(gr_context* ctx, uint8_t* rgba_dev, const float* z_dev, int32_t width, int32_t height,
+               float fog_start, float fog_end, const uint8_t* color4);
+/* Fused: every later frame of the context ends with Fog in the raster's
+ * write-back (after overlays and the crosshair), as Draw followed by Fog
+ * would; enable = 0 turns it off. */
+int32_t gr_context_set_fog(gr_context* ctx, int32_t enable, float fog_start, float fog_end,
+                           const uint8_t* color4);
 
 /* ---- timing helpers (CUDA events on the context stream) ---- */
 int32_t gr_context_event_record(gr_context* ctx, int32_t slot);  /* slot < 64 */

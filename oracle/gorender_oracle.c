@@ -757,6 +757,23 @@ static void draw_rect(Plot* p, int64_t x, int64_t y, int64_t w, int64_t h, const
     for (int64_t px = x; px < wadd(x, w); px++) plot(p, px, py, c);
 }
 
+/* FrameBuffer.Fog (rasterizer.go:193-207) with blendRGBA (185-191):
+ * uint8(float32(a)*(1-f) + float32(b)*f) per channel, alpha included. */
+void orc_fog(uint8_t* rgba, const float* z, int32_t width, int32_t height, float fog_start, float fog_end,
+             const uint8_t* color) {
+  const int64_t n = (int64_t)width * height;
+  for (int64_t i = 0; i < n; i++) {
+    const float depth = z[i];
+    if (depth >= fog_start) continue;
+    if (depth <= fog_end) {
+      memcpy(rgba + 4 * i, color, 4);
+      continue;
+    }
+    const float f = 1 - ((fog_end - depth) / (fog_end - fog_start));
+    for (int k = 0; k < 4; k++) rgba[4 * i + k] = orc_go_uint8((float)rgba[4 * i + k] * (1 - f) + (float)color[k] * f);
+  }
+}
+
 int orc_fb_line(uint8_t* rgba, int32_t width, int32_t height, int64_t x0, int64_t y0, int64_t x1, int64_t y1,
                 const uint8_t* color) {
   Plot p = {rgba, width, (int64_t)width * height, 0, height, 0};
@@ -868,6 +885,7 @@ int orc_draw_ids(const orc_item* items, int32_t nitems, const orc_frame* fr, uin
       }
     }
 
+  const uint32_t fl_all = fr->flags;
   DrawCtx c;
   memset(&c, 0, sizeof(c));
   c.items = items; c.nitems = nitems; c.fr = fr; c.rgba = rgba; c.z = z; c.ids = ids;
@@ -915,6 +933,17 @@ int orc_draw_ids(const orc_item* items, int32_t nitems, const orc_frame* fr, uin
       for (int k = 0; k < nt; k++) pthread_join(th[k], NULL);
     }
     if (c.band_err) err = c.band_err;
+    if (!err && (fl_all & ORC_CROSSHAIR)) {
+      /* FrameBuffer.CrossHair (rasterizer.go:209-217), drawn after the scene
+       * when the reference's demoMode is off (renderer.go:476-478) */
+      static const uint8_t kYellow[4] = {255, 255, 0, 255};
+      Plot pl = {rgba, fr->width, npx, 0, fr->height, 0};
+      const int64_t x = fr->width / 2, y = fr->height / 2;
+      draw_line(&pl, x - 5, y, x - 3, y, kYellow);
+      draw_line(&pl, x + 3, y, x + 5, y, kYellow);
+      draw_line(&pl, x, y - 5, x, y - 3, kYellow);
+      draw_line(&pl, x, y + 3, x, y + 5, kYellow);
+    }
   }
   for (int32_t i = 0; i < nitems; i++) free(c.lists[i].v);
   free(c.lists);

@@ -38,6 +38,9 @@ extern "C" {
 #define ORC_SHOW_TEXTURES 0x20u
 #define ORC_SHOW_EDGES 0x40u
 #define ORC_SHOW_VERTICES 0x80u
+/* Not a Renderer field: draws FrameBuffer.CrossHair after the scene, as Draw
+ * does when the reference's demoMode constant is false (renderer.go:476-478). */
+#define ORC_CROSSHAIR 0x100u
 
 /* Texture kinds (texture.go:12-17). */
 #define ORC_TEX_SOLID 0
@@ -180,6 +183,9 @@ int orc_fb_line(uint8_t* rgba, int32_t width, int32_t height, int64_t x0, int64_
                 const uint8_t* color);
 void orc_fb_rect(uint8_t* rgba, int32_t width, int32_t height, int64_t x, int64_t y, int64_t w, int64_t h,
                  const uint8_t* color);
+/* FrameBuffer.Fog (rasterizer.go:193-207) on an existing frame. */
+void orc_fog(uint8_t* rgba, const float* z, int32_t width, int32_t height, float fog_start, float fog_end,
+             const uint8_t* color);
 /* NewMesh face normals (mesh.go:53-60) and boundingBox (mesh.go:28-51). */
 void orc_mesh_face_normals(const float* pos, const int32_t* vidx, int32_t nf,
                            float* fnrm_out);

@@ -112,6 +112,7 @@ def lib():
         L.orc_fb_line.restype = C.c_int
         L.orc_fb_rect.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                   C.c_void_p]
+        L.orc_fog.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_void_p]
         L.orc_mesh_face_normals.argtypes = [fp, C.c_void_p, C.c_int32, fp]
         L.orc_mesh_bbox.argtypes = [fp, C.c_int32, fp]
         L.orc_world_matrix.argtypes = [fp, fp, fp, fp]
@@ -360,6 +361,15 @@ def draw_scene(scene, nthreads: int = 1, flags: Optional[int] = None, light=None
     st = lib().orc_draw(items, len(scene.objects), C.byref(fr), rgba.ctypes.data, z.ctypes.data,
                         C.byref(tpf), nthreads)
     return rgba, z, int(tpf.value), int(st)
+
+
+def fog(rgba: np.ndarray, z: np.ndarray, fog_start: float, fog_end: float, color) -> np.ndarray:
+    """FrameBuffer.Fog on a copy of rgba (H x W x 4 uint8) with z (H x W float32)."""
+    out = np.ascontiguousarray(rgba, np.uint8).copy()
+    zz = np.ascontiguousarray(z, np.float32)
+    col = (C.c_uint8 * 4)(*color)
+    lib().orc_fog(out.ctypes.data, zz.ctypes.data, out.shape[1], out.shape[0], fog_start, fog_end, col)
+    return out
 
 
 # ---- differentiable shading extension (FP64) ----

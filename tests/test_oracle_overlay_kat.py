@@ -92,3 +92,19 @@ def test_rect_at_origin_skips_index_zero():
     oracle.lib().orc_fb_rect(b.ctypes.data, W, H, -1, -1, 3, 3, MARK)
     # y = -1: indices -9..-7 (none); y = 0: -1 (none), 0 (skipped), 1; y = 1: 7, 8, 9
     assert _marked(b) == {(1, 0), (7, 0), (0, 1), (1, 1)}
+
+
+# ---- FrameBuffer.Fog (rasterizer.go:185-207) ----
+
+def test_fog_hand_computed():
+    # start 1.0, end 0.0: depth 0.25 blends with f = 1 - (0 - 0.25) / (0 - 1) = 0.75 (exact)
+    rgba = np.array([[[200, 100, 50, 255], [200, 100, 50, 255], [200, 100, 50, 255], [200, 100, 50, 255],
+                      [10, 20, 30, 40]]], np.uint8)
+    z = np.array([[0.25, 1.0, 0.0, -1.0, float("nan")]], np.float32)
+    out = oracle.fog(rgba, z, 1.0, 0.0, (100, 100, 100, 255))
+    # 200*.25 + 100*.75 = 125; 100; 50*.25 + 75 = 87.5 -> 87; 255*.25 + 255*.75 = 255
+    assert out[0, 0].tolist() == [125, 100, 87, 255]
+    assert out[0, 1].tolist() == [200, 100, 50, 255]   # depth >= start: unchanged
+    assert out[0, 2].tolist() == [100, 100, 100, 255]  # depth <= end: fog colour
+    assert out[0, 3].tolist() == [100, 100, 100, 255]  # background (Z = -1)
+    assert out[0, 4].tolist() == [0, 0, 0, 0]          # NaN depth: f = NaN, uint8(NaN) = 0
