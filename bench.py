@@ -232,6 +232,7 @@ def run_ours(args):
     N.check(L.gr_host_free(hp))
     e2e_value = faces * e2e_frames * ws / e2e_s / 1e6
 
+    present = bench_present(ctx, up, scene, e2e_frames)
     batched = bench_batched(ctx, args, local) if not args.skip_batched else None
     stress = bench_stress(ctx, args) if not args.skip_batched else None
     diff = bench_diff(local) if not args.skip_batched else None
@@ -262,6 +263,7 @@ def run_ours(args):
                      "frame_algorithmic_bytes": int(ab["frame"])},
         "gpu_launches": int(launches_per_frame * args.steps),
         "clocks": sampler.summary(),
+        "e2e_present": present,
         "batched_multiview": batched,
         "stress_1080p": stress,
         "diff_fwd_bwd": diff,
@@ -410,6 +412,38 @@ def bench_diff(device):
             "pixels": npx, "forward_ms": round(mf, 4), "backward_ms": round(mb, 4),
             "backward_over_forward": round(mb / mf, 3), "views_per_s": round(64 / ((mf + mb) * 1e-3), 1),
             "loss": loss, "reps": reps, "l2": "flushed between iterations"}
+
+
+def bench_present(ctx, up, scene, frames):
+    """The present loop of the reference (Draw, SwapBuffers, show the finished
+    frame while the next one renders) through gr_presenter_frame: each call
+    queues a frame and returns the previous one's pixels in host memory, the
+    device-to-host copy overlapping the next frame.  Wall clock, Python loop."""
+    import gorender_gb300 as gr
+    r = gr.Renderer(ctx, scene.width, scene.height)
+    r.FlatShading = bool(scene.flags & gr.FLAT_SHADING)
+    r.set_fov(up.fov)
+    objs = [gr.Object(h, o.scale, o.rotation, o.translation) for h, o in zip(up.mesh_handles, scene.objects)]
+    cam = gr.Camera(scene.camera.position, scene.camera.direction, scene.camera.up)
+    p = gr.Presenter(r)
+    for _ in range(5):
+        p.frame(objs, cam)
+    p.flush()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        rgba, _ = p.frame(objs, cam)
+    p.flush()
+    dt = time.perf_counter() - t0
+    import ctypes as C
+    from gorender_gb300 import _native as N
+    h2d, d2h = C.c_int64(), C.c_int64()
+    N.check(N.lib().gr_context_last_transfer_bytes(ctx.handle, C.byref(h2d), C.byref(d2h)))
+    p.close()
+    r.close()
+    return {"value": round(scene.num_triangles * frames / dt / 1e6, 3), "unit": "Mtris/s", "frames": frames,
+            "ms_per_frame": round(dt * 1e3 / frames, 4), "h2d_bytes_per_step": int(h2d.value),
+            "d2h_bytes_per_step": scene.width * scene.height * 4,
+            "note": "pixels only (the reference presents Pixels2); matrices built by the library per frame"}
 
 
 def bench_stress(ctx, args):

@@ -38,7 +38,8 @@ EXPORTS = [
     "gr_draw_views", "gr_context_view_tpf", "gr_batch_create", "gr_batch_run", "gr_batch_sync",
     "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_get_raster",
     "gr_context_autotune", "gr_diff_create", "gr_diff_forward", "gr_diff_backward", "gr_diff_buffers",
-    "gr_diff_destroy", "gr_fog", "gr_context_set_fog", "gr_renderer_fog",
+    "gr_diff_destroy", "gr_fog", "gr_context_set_fog", "gr_renderer_fog", "gr_presenter_create",
+    "gr_presenter_frame", "gr_presenter_flush", "gr_presenter_destroy",
 ]
 
 
@@ -174,6 +175,10 @@ def lib() -> C.CDLL:
             "gr_fog": [vp, vp, vp, i32, i32, C.c_float, C.c_float, vp],
             "gr_context_set_fog": [vp, i32, C.c_float, C.c_float, vp],
             "gr_renderer_fog": [vp, C.c_float, C.c_float, vp],
+            "gr_presenter_create": [vp, C.POINTER(vp)],
+            "gr_presenter_frame": [vp, C.POINTER(Object), i32, C.POINTER(Camera), C.POINTER(vp), C.POINTER(C.c_int64)],
+            "gr_presenter_flush": [vp, C.POINTER(vp), C.POINTER(C.c_int64)],
+            "gr_presenter_destroy": [vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)

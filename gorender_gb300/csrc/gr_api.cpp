@@ -554,16 +554,23 @@ uint64_t buffers_signature(const gr_context* c) {
   return h;
 }
 
-// Reads the frame result; grows buffers that overflowed.  Returns 1 when the
-// frame must be re-run.
+// Reads a frame's result; grows buffers that overflowed.  Returns 1 when the
+// frame must be re-run.  The kernels record a *_need value only when an
+// append did not fit, so any non-zero one means the frame is incomplete,
+// even if the buffers have grown since it was queued (asynchronous frames).
 int check_result(gr_context* c, const DevResult& r, int32_t* err) {
   *err = GR_OK;
   int rerun = 0;
-  if (r.bin_need > c->bin_cap) { c->want_bin_cap = next_pow2((uint64_t)r.bin_need + r.bin_need / 4); rerun = 1; }
-  if (r.rec_need > c->rec_cap) { c->want_rec_cap = r.rec_need + r.rec_need / 8; rerun = 1; }
-  if (r.big_need > c->big_cap) { c->want_big_cap = next_pow2((uint64_t)r.big_need + r.big_need / 4); rerun = 1; }
-  if (r.clip_need > c->clip_cap) { c->want_clip_cap = next_pow2((uint64_t)r.clip_need + r.clip_need / 4); rerun = 1; }
-  if (r.ovl_need > c->ovl_cap) { c->want_ovl_cap = next_pow2((uint64_t)r.ovl_need + r.ovl_need / 4); rerun = 1; }
+  auto grow = [&](uint32_t need, uint32_t cap, uint32_t& want, uint64_t size) {
+    if (!need) return;
+    rerun = 1;
+    if (need > cap) want = (uint32_t)std::min<uint64_t>(size, 0xFFFFFFFFull);
+  };
+  grow(r.bin_need, c->bin_cap, c->want_bin_cap, next_pow2((uint64_t)r.bin_need + r.bin_need / 4));
+  grow(r.rec_need, c->rec_cap, c->want_rec_cap, (uint64_t)r.rec_need + r.rec_need / 8);
+  grow(r.big_need, c->big_cap, c->want_big_cap, next_pow2((uint64_t)r.big_need + r.big_need / 4));
+  grow(r.clip_need, c->clip_cap, c->want_clip_cap, next_pow2((uint64_t)r.clip_need + r.clip_need / 4));
+  grow(r.ovl_need, c->ovl_cap, c->want_ovl_cap, next_pow2((uint64_t)r.ovl_need + r.ovl_need / 4));
   if (r.error & 1u) *err = fail(GR_ERR_CLIP_OVERFLOW, "a clipped polygon exceeded 9 vertices");
   if (r.error & 4u)
     *err = fail(GR_ERR_UNSUPPORTED, "an edge overlay line has more than %lld steps (a corner far off screen)",
@@ -1691,4 +1698,167 @@ int32_t gr_context_set_fog(gr_context* c, int32_t enable, float fog_start, float
   return GR_OK;
 }
 
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Headless present: two device framebuffers, copies on a second stream
+// ---------------------------------------------------------------------------
+struct gr_presenter {
+  gr_renderer* r = nullptr;
+  cudaStream_t copy = nullptr;
+  uint32_t* dev[2] = {nullptr, nullptr};
+  uint8_t* host[2] = {nullptr, nullptr};      // pinned
+  DevResult* res[2] = {nullptr, nullptr};     // pinned: each frame's counters
+  cudaEvent_t rendered[2] = {}, copied[2] = {};
+  std::vector<gr_draw_item> items[2];
+  bool queued[2] = {false, false};            // rendered + copy queued, not yet returned
+  int64_t frame = 0;
+};
+
+namespace {
+
+void presenter_free(gr_presenter* p) {
+  for (int b = 0; b < 2; ++b) {
+    dev_free(p->dev[b]);
+    if (p->host[b]) cudaFreeHost(p->host[b]);
+    if (p->res[b]) cudaFreeHost(p->res[b]);
+    if (p->rendered[b]) cudaEventDestroy(p->rendered[b]);
+    if (p->copied[b]) cudaEventDestroy(p->copied[b]);
+  }
+  if (p->copy) cudaStreamDestroy(p->copy);
+}
+
+// Queues frame buffer b: render on the context stream (after the copy that
+// last read buffer b), its counters, then the copy to host on the copy stream.
+int32_t presenter_enqueue(gr_presenter* p, int b) {
+  gr_renderer* r = p->r;
+  gr_context* c = r->ctx;
+  gr_frame_params fp;
+  std::memset(&fp, 0, sizeof(fp));
+  fp.width = r->width;
+  fp.height = r->height;
+  fp.flags = r->flags;
+  screen_matrix(r->width, r->height, fp.screen);
+  std::memcpy(fp.light, r->light, sizeof(fp.light));
+  CK(cudaStreamWaitEvent(c->stream, p->copied[b], 0));
+  ViewIn v{&fp, p->dev[b], r->z};
+  Prepared pr;
+  int32_t st = prepare(c, &v, 1, p->items[b].data(), (int32_t)p->items[b].size(), false, pr);
+  if (st) return st;
+  if ((st = launch(c, pr.a))) return st;
+  CK(cudaMemcpyAsync(p->res[b], c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaEventRecord(p->rendered[b], c->stream));
+  CK(cudaStreamWaitEvent(p->copy, p->rendered[b], 0));
+  CK(cudaMemcpyAsync(p->host[b], p->dev[b], (size_t)r->width * r->height * 4, cudaMemcpyDeviceToHost, p->copy));
+  CK(cudaEventRecord(p->copied[b], p->copy));
+  p->queued[b] = true;
+  return GR_OK;
+}
+
+// Waits for buffer b's copy; renders it again while its buffers overflowed.
+int32_t presenter_collect(gr_presenter* p, int b, const uint8_t** rgba, int64_t* tpf) {
+  gr_context* c = p->r->ctx;
+  for (int attempt = 0; attempt < 5; ++attempt) {
+    CK(cudaEventSynchronize(p->copied[b]));
+    int32_t err;
+    const int rerun = check_result(c, *p->res[b], &err);
+    if (err) return err;
+    if (!rerun) {
+      p->queued[b] = false;
+      if (rgba) *rgba = p->host[b];
+      if (tpf) *tpf = (int64_t)p->res[b]->tpf;
+      return GR_OK;
+    }
+    int32_t st = presenter_enqueue(p, b);  // the buffers grow in prepare()
+    if (st) return st;
+  }
+  return fail(GR_ERR_OUT_OF_MEMORY, "frame buffers kept overflowing after resizing");
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gr_presenter_create(gr_renderer* r, gr_presenter** out) {
+  if (!r || !out) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  gr_context* c = r->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  gr_presenter* p = new (std::nothrow) gr_presenter();
+  if (!p) return fail(GR_ERR_OUT_OF_MEMORY, "presenter allocation");
+  p->r = r;
+  const size_t px = (size_t)r->width * r->height;
+  cudaError_t e = cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking);
+  int32_t st = e == cudaSuccess ? GR_OK : fail(GR_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e));
+  for (int b = 0; b < 2 && !st; ++b) {
+    if ((st = dev_alloc(&p->dev[b], px))) break;
+    e = cudaMallocHost((void**)&p->host[b], px * 4);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->res[b], sizeof(DevResult));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->rendered[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->copied[b], cudaEventDisableTiming);
+    if (e != cudaSuccess) st = fail(GR_ERR_CUDA, "presenter buffers: %s", cudaGetErrorString(e));
+  }
+  if (st) {
+    presenter_free(p);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return GR_OK;
+}
+
+int32_t gr_presenter_frame(gr_presenter* p, const gr_object* objs, int32_t n, const gr_camera* cam,
+                           const uint8_t** prev_rgba, int64_t* prev_tpf) {
+  if (!p || !cam || n < 0 || (n > 0 && !objs)) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  gr_renderer* r = p->r;
+  gr_context* c = r->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  const int b = (int)(p->frame & 1), prev = b ^ 1;
+  if (p->queued[b]) {  // never returned (a flush was skipped): collect it first
+    int32_t st = presenter_collect(p, b, nullptr, nullptr);
+    if (st) return st;
+  }
+  std::vector<gr_draw_item>& items = p->items[b];
+  items.assign((size_t)n, gr_draw_item{});
+  for (int i = 0; i < n; ++i) {
+    items[i].mesh = objs[i].mesh;
+    object_matrices(objs[i].scale, objs[i].rotation, objs[i].translation, cam->position, cam->direction, cam->up,
+                    r->width, r->height, r->fov_y, items[i].mvp, items[i].world);
+  }
+  int32_t st = presenter_enqueue(p, b);
+  if (st) return st;
+  p->frame += 1;
+  if (prev_rgba) *prev_rgba = nullptr;
+  if (prev_tpf) *prev_tpf = -1;
+  if (!p->queued[prev]) return GR_OK;
+  return presenter_collect(p, prev, prev_rgba, prev_tpf);
+}
+
+int32_t gr_presenter_flush(gr_presenter* p, const uint8_t** rgba, int64_t* tpf) {
+  if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "presenter is NULL");
+  gr_context* c = p->r->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  if (rgba) *rgba = nullptr;
+  if (tpf) *tpf = -1;
+  const int last = (int)((p->frame + 1) & 1);  // the most recently queued buffer
+  if (!p->queued[last]) return GR_OK;
+  return presenter_collect(p, last, rgba, tpf);
+}
+
+int32_t gr_presenter_destroy(gr_presenter* p) {
+  if (!p) return GR_OK;
+  {
+    std::lock_guard<std::mutex> lk(p->r->ctx->mu);
+    cudaSetDevice(p->r->ctx->device);
+    cudaStreamSynchronize(p->r->ctx->stream);
+    if (p->copy) cudaStreamSynchronize(p->copy);
+    presenter_free(p);
+  }
+  delete p;
+  return GR_OK;
+}
 }  // extern "C"

@@ -105,7 +105,9 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
-        self._batches = []  # closed before the context: a batch must not outlive it
+        # objects living on this context (batches, diffs, renderers, presenters):
+        # closed before it, newest first, since none may outlive the context
+        self._batches = []
         N.check(N.lib().gr_context_create(device, C.byref(self._h)))
 
     @property
@@ -113,7 +115,7 @@ class Context:
         return self._h
 
     def close(self):
-        for b in list(self._batches):
+        for b in reversed(list(self._batches)):
             b.close()
         self._batches = []
         if self._h:
@@ -274,6 +276,26 @@ class Object:
         self.Mesh, self.Scale, self.Rotation, self.Translation = mesh, scale, rotation, translation
 
 
+def _c_objects(objects: Sequence[Object]):
+    objs = (N.Object * max(1, len(objects)))()
+    for i, o in enumerate(objects):
+        objs[i].mesh = o.Mesh
+        for k in range(3):
+            objs[i].scale[k] = o.Scale[k]
+            objs[i].rotation[k] = o.Rotation[k]
+            objs[i].translation[k] = o.Translation[k]
+    return objs
+
+
+def _c_camera(camera: Camera):
+    cam = N.Camera()
+    for k in range(3):
+        cam.position[k] = camera.Position[k]
+        cam.direction[k] = camera.Direction[k]
+        cam.up[k] = camera.Up[k]
+    return cam
+
+
 class Renderer:
     """NewFrameBuffer(width, height) + NewRenderer(fb) (rasterizer.go:15, renderer.go:114)."""
 
@@ -289,6 +311,7 @@ class Renderer:
         object.__setattr__(self, "_h", h)
         object.__setattr__(self, "width", width)
         object.__setattr__(self, "height", height)
+        ctx._batches.append(self)
 
     def _flags(self) -> int:
         f = C.c_uint32()
@@ -318,18 +341,7 @@ class Renderer:
 
     def draw(self, objects: Sequence[Object], camera: Camera) -> None:
         """(*Renderer).Draw (renderer.go:443-483)."""
-        objs = (N.Object * max(1, len(objects)))()
-        for i, o in enumerate(objects):
-            objs[i].mesh = o.Mesh
-            for k in range(3):
-                objs[i].scale[k] = o.Scale[k]
-                objs[i].rotation[k] = o.Rotation[k]
-                objs[i].translation[k] = o.Translation[k]
-        cam = N.Camera()
-        for k in range(3):
-            cam.position[k] = camera.Position[k]
-            cam.direction[k] = camera.Direction[k]
-            cam.up[k] = camera.Up[k]
+        objs, cam = _c_objects(objects), _c_camera(camera)
         N.check(N.lib().gr_renderer_draw(self._h, objs, len(objects), C.byref(cam)))
 
     @property
@@ -357,6 +369,14 @@ class Renderer:
         if self._h:
             N.lib().gr_renderer_destroy(self._h)
             object.__setattr__(self, "_h", C.c_void_p())
+        if self in self._ctx._batches:
+            self._ctx._batches.remove(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---- scenes ----
@@ -529,6 +549,49 @@ class Diff:
             self._h = C.c_void_p()
         if self in self.ctx._batches:
             self.ctx._batches.remove(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Presenter:
+    """Double-buffered headless present (gr_presenter_*): ``frame(objects, camera)``
+    queues a Draw and returns the previous frame (a copy of its pixels, H x W x 4,
+    and its TPF), or (None, -1) on the first call; ``flush()`` returns the last."""
+
+    def __init__(self, renderer: "Renderer"):
+        self.renderer = renderer
+        self._h = C.c_void_p()
+        N.check(N.lib().gr_presenter_create(renderer._h, C.byref(self._h)))
+        renderer._ctx._batches.append(self)
+
+    def _take(self, ptr, tpf):
+        if not ptr:
+            return None, -1
+        n = self.renderer.width * self.renderer.height * 4
+        arr = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_uint8)), shape=(n,))
+        return arr.reshape(self.renderer.height, self.renderer.width, 4).copy(), int(tpf.value)
+
+    def frame(self, objects: Sequence[Object], camera: Camera):
+        ptr, tpf = C.c_void_p(), C.c_int64()
+        N.check(N.lib().gr_presenter_frame(self._h, _c_objects(objects), len(objects), C.byref(_c_camera(camera)),
+                                           C.byref(ptr), C.byref(tpf)))
+        return self._take(ptr.value, tpf)
+
+    def flush(self):
+        ptr, tpf = C.c_void_p(), C.c_int64()
+        N.check(N.lib().gr_presenter_flush(self._h, C.byref(ptr), C.byref(tpf)))
+        return self._take(ptr.value, tpf)
+
+    def close(self):
+        if self._h:
+            N.lib().gr_presenter_destroy(self._h)
+            self._h = C.c_void_p()
+        if self in self.renderer._ctx._batches:
+            self.renderer._ctx._batches.remove(self)
 
     def __del__(self):
         try:

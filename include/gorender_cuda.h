@@ -219,6 +219,24 @@ int32_t gr_renderer_tpf(gr_renderer* r, int64_t* tpf);
 /* FrameBuffer.Fog (rasterizer.go:193-207) on the renderer's last frame. */
 int32_t gr_renderer_fog(gr_renderer* r, float fog_start, float fog_end, const uint8_t* color4);
 
+/* ---- headless present (double buffer) ----
+ * FrameBuffer.SwapBuffers (rasterizer.go:32-34) and the reference's present
+ * loop (main.go:221-228, 297): frames render into two device framebuffers in
+ * turn; each finished frame is copied to page-locked host memory on a second
+ * stream while the next frame renders.  The Z buffer stays single, as in the
+ * reference. */
+typedef struct gr_presenter gr_presenter;
+int32_t gr_presenter_create(gr_renderer* r, gr_presenter** out);
+/* Queues Draw(objects, camera) (the renderer's flags, FOV and light) and
+ * returns the previous frame's pixels (host, width*height*4 bytes, valid
+ * until the next call) and its TPF; on the first call *prev_rgba is NULL.
+ * A frame whose buffers overflowed is rendered again before it is returned. */
+int32_t gr_presenter_frame(gr_presenter* p, const gr_object* objects, int32_t num_objects, const gr_camera* camera,
+                           const uint8_t** prev_rgba, int64_t* prev_tpf);
+/* Waits for the last queued frame and returns it (NULL when none is queued). */
+int32_t gr_presenter_flush(gr_presenter* p, const uint8_t** rgba, int64_t* tpf);
+int32_t gr_presenter_destroy(gr_presenter* p);
+
 /* ---- fog (rasterizer.go:185-207) ----
  * FrameBuffer.Fog: pixels with depth >= fog_start keep their colour, those
  * with depth <= fog_end take color4, the rest blend by
