@@ -251,7 +251,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "faces": faces, "width": W, "height": H,
                    "binned_triangles": int(tpf.value), "parallelism": f"replicas x{ws}",
                    "l2": "flushed between frames (512 MiB write outside the timed events)",
-                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_entries": ctx.raster()[0]},
+                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_cost": ctx.raster()[0]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
                 "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
@@ -473,7 +473,7 @@ def bench_stress(ctx, args):
     ms = statistics.median(t)
     return {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
             "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
-            "frames": frames, "tile_size": ctx.tuning()[0], "slice_entries": ctx.raster()[0]}
+            "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0]}
 
 
 def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):

@@ -90,6 +90,7 @@ struct gr_context {
   uint32_t key_cap = 0;
   uint32_t* bins = nullptr;
   uint32_t* bin_count = nullptr;
+  uint32_t* tile_cost = nullptr;    // per tile: boxes of its large entries (k_plan's cost estimate)
   uint32_t bin_cap = 0;
   uint32_t tiles_cap = 0;
   uint2* big = nullptr;             // multi-tile queue: (record, view)
@@ -119,7 +120,7 @@ struct gr_context {
   int raster_waves = 1;             // persistent raster CTAs = SMs x resident CTAs x waves
   int last_views = 0;               // views of the last batched draw
   float tuned_ms = 0.0f;            // best batch time seen by the autotuner
-  uint32_t slice_entries = kDefaultSliceEntries;
+  uint32_t slice_cost = kDefaultSliceCost;
   DevWork* work = nullptr;
   DevResult* d_result = nullptr;
   DevResult* h_result = nullptr;  // pinned
@@ -236,10 +237,13 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
     if ((st = sync())) return st;
     uint32_t nt = std::max(tiles, c->tiles_cap);
     uint32_t nc = std::max(want_bin, c->bin_cap);
-    dev_free(c->bins); dev_free(c->bin_count);
+    dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost);
     c->tiles_cap = 0; c->bin_cap = 0;
-    if ((st = dev_alloc(&c->bins, (size_t)nt * nc)) || (st = dev_alloc(&c->bin_count, nt))) return st;
+    if ((st = dev_alloc(&c->bins, (size_t)nt * nc)) || (st = dev_alloc(&c->bin_count, nt)) ||
+        (st = dev_alloc(&c->tile_cost, nt)))
+      return st;
     CK(cudaMemsetAsync(c->bin_count, 0, sizeof(uint32_t) * nt, c->stream));
+    CK(cudaMemsetAsync(c->tile_cost, 0, sizeof(uint32_t) * nt, c->stream));
     if (nt > c->gkey_tiles) {
       dev_free(c->gkey); dev_free(c->tile_done);
       c->gkey_tiles = 0;
@@ -505,10 +509,11 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.rec_of_key = c->rec_of_key;
   a.bins = c->bins;
   a.bin_count = c->bin_count;
+  a.tile_cost = c->tile_cost;
   a.big = c->big;
   a.gkey = c->gkey;
   a.tile_done = c->tile_done;
-  a.slice_entries = c->slice_entries;
+  a.slice_cost = c->slice_cost;
   a.clip = c->clip;
   a.clip_cap = c->clip_cap;
   a.vlight = c->vlight;
@@ -539,11 +544,11 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
 // signature no longer matches must be captured again before it runs.
 uint64_t buffers_signature(const gr_context* c) {
   const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->wide, (uintptr_t)c->tcol,
-                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->gkey,
+                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->gkey,
                           (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->big, (uintptr_t)c->vlight,
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, c->rec_cap, c->key_cap, c->bin_cap,
-                          c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_entries,
+                          c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_cost,
                           (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key,
                           c->ovl_cap};
   uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
@@ -680,7 +685,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->d_texs); dev_free(c->d_items);
   if (c->h_items) cudaFreeHost(c->h_items);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
-  dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->big);
+  dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
   dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan);
   dev_free(c->ovl); dev_free(c->ovl_key);
@@ -1005,13 +1010,13 @@ int32_t batch_autotune(gr_batch* b) {
   struct Cfg {
     int shift, slice, waves;
   };
-  // tile size (and with it the raster CTA: TS*TS/4 threads) x bin entries per raster slice
-  const Cfg cands[] = {{5, 128, 1}, {5, 64, 1}, {5, 256, 1}, {4, 32, 1}, {4, 64, 1}, {4, 128, 1}, {4, 256, 1}};
+  // tile size (and with it the raster CTA: TS*TS/4 threads) x raster cost per slice
+  const Cfg cands[] = {{5, 8192, 1}, {5, 16384, 1}, {5, 32768, 1}, {4, 2048, 1}, {4, 4096, 1}, {4, 8192, 1}};
   Cfg best = cands[0];
   float best_ms = 1e30f;
   for (const Cfg& k : cands) {
     c->tile_shift = k.shift;
-    c->slice_entries = (uint32_t)k.slice;
+    c->slice_cost = (uint32_t)k.slice;
     c->raster_waves = k.waves;
     int32_t st = batch_run_plain(b, nullptr);  // warm up and size the buffers
     if (st) return st;
@@ -1027,7 +1032,7 @@ int32_t batch_autotune(gr_batch* b) {
     }
   }
   c->tile_shift = best.shift;
-  c->slice_entries = (uint32_t)best.slice;
+  c->slice_cost = (uint32_t)best.slice;
   c->raster_waves = best.waves;
   int32_t st = batch_run_plain(b, nullptr);
   if (st) return st;
@@ -1105,12 +1110,12 @@ int32_t gr_batch_sync(gr_batch* b) {
   return fail(GR_ERR_OUT_OF_MEMORY, "batch buffers kept overflowing after resizing");
 }
 
-int32_t gr_batch_tuning(gr_batch* b, int32_t* tile_size, int32_t* slice_entries, int32_t* raster_waves,
+int32_t gr_batch_tuning(gr_batch* b, int32_t* tile_size, int32_t* slice_cost, int32_t* raster_waves,
                         int32_t* bin_capacity, float* tuned_ms) {
   if (!b) return fail(GR_ERR_INVALID_ARGUMENT, "batch is NULL");
   gr_context* c = b->ctx;
   if (tile_size) *tile_size = 1 << c->tile_shift;
-  if (slice_entries) *slice_entries = (int32_t)c->slice_entries;
+  if (slice_cost) *slice_cost = (int32_t)c->slice_cost;
   if (raster_waves) *raster_waves = c->raster_waves;
   if (bin_capacity) *bin_capacity = (int32_t)c->bin_cap;
   if (tuned_ms) *tuned_ms = c->tuned_ms;
@@ -1330,19 +1335,19 @@ int32_t gr_context_set_tuning(gr_context* c, int32_t tile_size, int32_t bin_capa
   return GR_OK;
 }
 
-int32_t gr_context_set_raster(gr_context* c, int32_t slice_entries, int32_t raster_waves) {
+int32_t gr_context_set_raster(gr_context* c, int32_t slice_cost, int32_t raster_waves) {
   if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "ctx is NULL");
-  if (slice_entries < 0 || raster_waves < 0 || raster_waves > 16)
+  if (slice_cost < 0 || raster_waves < 0 || raster_waves > 16)
     return fail(GR_ERR_INVALID_ARGUMENT, "bad raster tuning");
   std::lock_guard<std::mutex> lk(c->mu);
-  if (slice_entries) c->slice_entries = (uint32_t)slice_entries;
+  if (slice_cost) c->slice_cost = (uint32_t)slice_cost;
   if (raster_waves) c->raster_waves = raster_waves;
   return GR_OK;
 }
 
-int32_t gr_context_get_raster(gr_context* c, int32_t* slice_entries, int32_t* raster_waves) {
-  if (!c || !slice_entries || !raster_waves) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
-  *slice_entries = (int32_t)c->slice_entries;
+int32_t gr_context_get_raster(gr_context* c, int32_t* slice_cost, int32_t* raster_waves) {
+  if (!c || !slice_cost || !raster_waves) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *slice_cost = (int32_t)c->slice_cost;
   *raster_waves = c->raster_waves;
   return GR_OK;
 }

@@ -18,7 +18,9 @@ constexpr int kProjectThreads = 256;
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
 constexpr int kStageSlots = 3;                // pinned staging slots for back-to-back async draws
 constexpr int kRasterMaxSlices = 32;          // CTAs that may share one tile's bin
-constexpr int kDefaultSliceEntries = 128;     // bin entries per slice before a tile is split
+constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a tile is split
+constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
+constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 
 // Texture table entry (texture.go:19-26).
@@ -160,7 +162,8 @@ struct FrameArgs {
   TriColor* tcol;
   uint32_t* rec_of_key;             // order key -> record index
   uint32_t* bins;                   // tiles x bin_cap record indices
-  uint32_t* bin_count;              // per tile
+  uint32_t* bin_count;              // per tile: entries
+  uint32_t* tile_cost;              // per tile: tile-clipped box pixels of entries larger than kSmallBox
   uint2* big;                       // multi-tile queue: (record, view)
   uint2* clip;                      // (item, face) pairs for the general clipper
   uint32_t clip_cap;
@@ -168,7 +171,7 @@ struct FrameArgs {
   int light_blocks;                 // k_light grid (0: no Gouraud item)
   unsigned long long* gkey;         // tiles x 1024 merged visibility keys of split tiles (zero when idle)
   uint32_t* tile_done;              // per tile: slices finished (zero when idle)
-  uint32_t slice_entries;           // bin entries per slice
+  uint32_t slice_cost;              // raster cost per slice (k_plan splits costlier tiles)
   DevWork* work;
   DevResult* result;
   unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)

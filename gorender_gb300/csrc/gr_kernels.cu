@@ -307,6 +307,23 @@ __device__ __forceinline__ float zrec_of(float e12f, float e20f, float sumf, flo
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Tile-clipped pixel box of a triangle with box [bx0,bx1] x [by0,by1] in
+// tile (tx, ty).
+__device__ __forceinline__ uint32_t tile_box(int bx0, int bx1, int by0, int by1, uint32_t tx, uint32_t ty, int sh) {
+  const int ts = 1 << sh;
+  const int x0 = max(bx0, (int)(tx << sh)), x1 = min(bx1, (int)(tx << sh) + ts - 1);
+  const int y0 = max(by0, (int)(ty << sh)), y1 = min(by1, (int)(ty << sh) + ts - 1);
+  return (uint32_t)(max(0, x1 - x0 + 1) * max(0, y1 - y0 + 1));
+}
+
+// Reserves one bin entry of tile `tile` for a triangle whose tile-clipped box
+// holds `box` pixels; boxes beyond kSmallBox add their area to the tile's
+// raster cost estimate (small ones count kEntryCost each, in k_plan).
+__device__ __forceinline__ uint32_t bin_append(const FrameArgs& a, uint32_t tile, uint32_t box) {
+  if (box > (uint32_t)kSmallBox) atomicAdd(&a.tile_cost[tile], box);
+  return atomicAdd(&a.bin_count[tile], 1u);
+}
+
 // Appends record r to tile t's bin; over capacity the position is recorded
 // so the host can grow the bins and re-run the frame.
 __device__ __forceinline__ void bin_store(const FrameArgs& a, uint32_t tile, uint32_t pos, uint32_t r) {
@@ -425,7 +442,7 @@ __device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const
     for (uint32_t ty = ty0; ty <= ty1; ++ty)
       for (uint32_t tx = tx0; tx <= tx1; ++tx) {
         const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-        bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+        bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, a.tile_shift)), r);
       }
   } else {
     const uint32_t q = atomicAdd(&a.work->nbig, 1u);
@@ -593,10 +610,12 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
   const uint32_t r = base + __popc(em & ((1u << lane) - 1u));
   const bool ok = emit && r < a.rec_cap;
   uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
+  int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
   if (ok) {
     Setup s;
     setup_tri(s0, s1, s2, W, H, s);
     write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
+    pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
     tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
     tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
     ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
@@ -612,6 +631,8 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
     const int leader = __ffs(grp) - 1;
     const unsigned rank = __popc(grp & ((1u << lane) - 1u));
     uint32_t pos = 0;
+    const uint32_t box = (uint32_t)((pbx1 - pbx0 + 1) * (pby1 - pby0 + 1));
+    if (box > (uint32_t)kSmallBox) atomicAdd(&a.tile_cost[tile], box);
     if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
     pos = __shfl_sync(grp, pos, leader) + rank;
     bin_store(a, tile, pos, r);
@@ -621,7 +642,7 @@ __global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) 
     for (uint32_t ty = ty0; ty <= ty1; ++ty)
       for (uint32_t tx = tx0; tx <= tx1; ++tx) {
         const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-        bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+        bin_store(a, tile, bin_append(a, tile, tile_box(pbx0, pbx1, pby0, pby1, tx, ty, a.tile_shift)), r);
       }
   }
   // more: the multi-tile queue, one atomic per warp
@@ -803,7 +824,7 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
         if (e01 >= 0 || e12 >= 0 || e20 >= 0) continue;
       }
       const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-      bin_store(a, tile, atomicAdd(&a.bin_count[tile], 1u), r);
+      bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, sh)), r);
     }
   }
 }
@@ -916,9 +937,24 @@ struct RasterShape {
 
 // Exact depth test of one covered pixel: zRec in the reference's order,
 // then a 64-bit max of (ordered zRec, draw-order key) into the tile's keys.
+//
+// Early out: at a covered pixel the barycentrics are e/sum of adjusted edge
+// values that are all negative, so they lie in [0, 1] (to rounding) and
+// zRec = -(al/w0 + be/w1 + ga/w2) <= (1 / min|w|) * (1 + ~1e-6) when every w
+// is negative (in front of the camera).  A candidate whose bound stays below
+// the depth the pixel already holds, with a 1e-5 margin for the roundings,
+// loses strictly (ties, where draw order decides, are never skipped), so its
+// five divisions are not needed.
 template <int TS>
 __device__ __forceinline__ void depth_candidate(unsigned long long* skey, const TriRaster& t, const TriWide* wide,
                                                 uint32_t r, int x, int y, int tx0, int ty0) {
+  unsigned long long* p = skey + (y - ty0) * RasterShape<TS>::kStride + (x - tx0);
+  const unsigned long long cur = *(volatile unsigned long long*)p;
+  const uint32_t o = (uint32_t)(cur >> 32);
+  if (o & 0x80000000u) {  // the pixel holds a depth >= +0
+    const float wmin = fminf(fminf(-t.w0, -t.w1), -t.w2);
+    if (wmin > 0.0f && __fmul_rn(__uint_as_float(o & 0x7FFFFFFFu), wmin) > 1.00001f) return;
+  }
   bool inside;
   float e12f, e20f;
   edges_at(t, wide, r, x, y, inside, e12f, e20f);
@@ -926,7 +962,6 @@ __device__ __forceinline__ void depth_candidate(unsigned long long* skey, const 
   float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
   if (!(z >= -1.0f)) return;  // rasterizer.go:156 against the cleared Z of -1
   unsigned long long k = depth_key(z, t.key);
-  unsigned long long* p = skey + (y - ty0) * RasterShape<TS>::kStride + (x - tx0);
   if (k > *(volatile unsigned long long*)p) atomicMax(p, k);
 }
 
@@ -1022,9 +1057,12 @@ __device__ __forceinline__ void walk_blocks(CandQueue<TS>& q, unsigned long long
   }
 }
 
-// Number of raster slices of a tile holding n bin entries.
-__device__ __forceinline__ uint32_t tile_slices(const FrameArgs& a, uint32_t n) {
-  return min((uint32_t)kRasterMaxSlices, max(1u, (n + a.slice_entries - 1) / a.slice_entries));
+// Number of raster slices of a tile holding n bin entries of estimated total
+// cost `cost` (kEntryCost per entry plus the boxes of the large ones): about
+// one slice per slice_cost, at most kRasterMaxSlices, at least 4 entries each.
+__device__ __forceinline__ uint32_t tile_slices(const FrameArgs& a, uint32_t n, uint32_t cost) {
+  const uint32_t by_cost = (uint32_t)(((unsigned long long)cost + a.slice_cost - 1) / a.slice_cost);
+  return max(1u, min(min(by_cost, (uint32_t)kRasterMaxSlices), (n + 3u) / 4u));
 }
 
 template <int TS>
@@ -1063,7 +1101,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   // A tile's bin is split into up to kRasterMaxSlices slices, one work item each.
   const uint32_t count = a.bin_count[tile];
   const uint32_t n = min(count, a.bin_cap);
-  const uint32_t nslices = tile_slices(a, n);
+  const uint32_t nslices = tile_slices(a, n, count * (uint32_t)kEntryCost + a.tile_cost[tile]);
   if (slice >= nslices) return;
   const uint32_t per = (((n + nslices - 1) / nslices) + 31u) & ~31u;
   const uint32_t lo = min(n, slice * per), hi = min(n, lo + per);
@@ -1329,7 +1367,10 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       }
     }
   }
-  if (tid == 0) a.bin_count[tile] = 0;  // ready for the next frame
+  if (tid == 0) {  // ready for the next frame
+    a.bin_count[tile] = 0u;
+    a.tile_cost[tile] = 0u;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1410,10 +1451,12 @@ __global__ void __launch_bounds__(256) k_overlay(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_plan: the raster work queue.  One thread per global tile: a tile whose
-// bin needs several slices contributes one item per slice to the front of
-// the queue (heavy tiles start first), any other tile one item to the back.
-// One atomic per CTA reserves each part; no ordering between CTAs is needed.
+// k_plan: the raster work queue.  One thread per global tile.  A tile's
+// estimated cost (kEntryCost per bin entry plus the tile-clipped boxes of its
+// large triangles) decides its number of slices (about one per slice_cost);
+// split tiles and tiles worth at least half a slice go to the front of the
+// queue (heavy work starts first), the rest to the back.  One atomic per CTA
+// reserves each part; no ordering between CTAs is needed.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   __shared__ uint32_t s_nf, s_nb, s_bf, s_bb, s_max;
@@ -1426,11 +1469,15 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   __syncthreads();
   const bool valid = tile < a.total_tiles;
   const uint32_t count = valid ? a.bin_count[tile] : 0u;
-  const uint32_t ns = valid ? tile_slices(a, min(count, a.bin_cap)) : 0u;
+  const uint32_t cost = valid ? count * (uint32_t)kEntryCost + a.tile_cost[tile] : 0u;
+  const uint32_t ns = valid ? tile_slices(a, min(count, a.bin_cap), cost) : 0u;
+  // heavy items (split tiles, or whole tiles worth half a slice) go to the
+  // front of the queue so that they start first; the rest to the back
+  const bool heavy = ns > 1 || cost >= a.slice_cost / 2u;
   uint32_t mf = 0, mb = 0;
   if (valid) {
     atomicMax(&s_max, count);
-    if (ns > 1) mf = atomicAdd(&s_nf, ns);
+    if (heavy) mf = atomicAdd(&s_nf, ns);
     else mb = atomicAdd(&s_nb, 1u);
   }
   __syncthreads();
@@ -1441,7 +1488,7 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   }
   __syncthreads();
   if (!valid) return;
-  if (ns > 1) {
+  if (heavy) {
     for (uint32_t k = 0; k < ns; ++k) a.plan[s_bf + mf + k] = make_uint2(tile, k);
   } else {
     a.plan[a.plan_cap - 1u - (s_bb + mb)] = make_uint2(tile, 0u);

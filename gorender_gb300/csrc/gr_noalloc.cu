@@ -55,7 +55,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
-  size_t items, texs, views, view_tpf, view_tpf_out, plan, rast, shade, wide, tcol, keys, bins, bin_count, big, clip,
+  size_t items, texs, views, view_tpf, view_tpf_out, plan, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip,
       vlight, gkey, tile_done, work, result, end;
 };
 
@@ -75,6 +75,7 @@ constexpr Layout make_layout() {
   l.keys = o; o += up256(sizeof(uint32_t) * kKeyCap);
   l.bins = o; o += up256(sizeof(uint32_t) * kTiles * kBinCap);
   l.bin_count = o; o += up256(sizeof(uint32_t) * kTiles);
+  l.tile_cost = o; o += up256(sizeof(uint32_t) * kTiles);
   l.big = o; o += up256(sizeof(uint2) * kQueueCap);
   l.clip = o; o += up256(sizeof(uint2) * kQueueCap);
   l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
@@ -230,7 +231,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.big_cap = kQueueCap;
   a.key_cap = kKeyCap;
   a.clip_cap = kQueueCap;
-  a.slice_entries = kDefaultSliceEntries;
+  a.slice_cost = kDefaultSliceCost;
   a.light_blocks = light_blocks;
   a.items = (const DevItem*)(base + kLayout.items);
   a.texs = (const DevTex*)(base + kLayout.texs);
@@ -242,6 +243,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.rec_of_key = (uint32_t*)(base + kLayout.keys);
   a.bins = (uint32_t*)(base + kLayout.bins);
   a.bin_count = (uint32_t*)(base + kLayout.bin_count);
+  a.tile_cost = (uint32_t*)(base + kLayout.tile_cost);
   a.big = (uint2*)(base + kLayout.big);
   a.clip = (uint2*)(base + kLayout.clip);
   a.vlight = (float*)(base + kLayout.vlight);
@@ -258,6 +260,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   // The array keeps the previous call's contents: zero what the kernels
   // expect to find zeroed (counters, bin counts, split-tile keys).
   e = cudaMemsetAsync(base + kLayout.bin_count, 0, sizeof(uint32_t) * tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.tile_cost, 0, sizeof(uint32_t) * tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.gkey, 0, sizeof(unsigned long long) * tiles * 1024, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.tile_done, 0, sizeof(uint32_t) * tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.work, 0, sizeof(DevWork), s);

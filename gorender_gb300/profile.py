@@ -106,7 +106,7 @@ def main():
     ap.add_argument("--views", type=int, default=64, help="views of the diff workload")
     ap.add_argument("--autotune", action="store_true", help="run the library autotuner first")
     ap.add_argument("--tile", type=int, default=0, help="raster tile size (16 or 32; 0 keeps the default)")
-    ap.add_argument("--slice", type=int, default=0, help="bin entries per raster slice (0 keeps the default)")
+    ap.add_argument("--slice", type=int, default=0, help="raster cost per slice (0 keeps the default)")
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args()
     if args.scene == "batch":

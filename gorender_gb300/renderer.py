@@ -205,7 +205,7 @@ class Context:
         return int(t.value), int(b.value)
 
     def raster(self) -> Tuple[int, int]:
-        """(bin entries per raster slice, persistent-raster waves)."""
+        """(raster cost per slice, persistent-raster waves)."""
         s, w = C.c_int32(), C.c_int32()
         N.check(N.lib().gr_context_get_raster(self._h, C.byref(s), C.byref(w)))
         return int(s.value), int(w.value)
@@ -447,7 +447,7 @@ class Batch:
         t, s, w, b = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         ms = C.c_float()
         N.check(N.lib().gr_batch_tuning(self._h, C.byref(t), C.byref(s), C.byref(w), C.byref(b), C.byref(ms)))
-        return {"tile_size": t.value, "slice_entries": s.value, "raster_waves": w.value,
+        return {"tile_size": t.value, "slice_cost": s.value, "raster_waves": w.value,
                 "bin_capacity": b.value, "tuned_ms": ms.value}
 
     def view_tpf(self):

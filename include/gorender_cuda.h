@@ -171,7 +171,7 @@ int32_t gr_batch_create(gr_context* ctx, const gr_view* views, int32_t num_views
                         gr_batch** out);
 int32_t gr_batch_run(gr_batch* batch);
 int32_t gr_batch_sync(gr_batch* batch);
-int32_t gr_batch_tuning(gr_batch* batch, int32_t* tile_size, int32_t* slice_entries,
+int32_t gr_batch_tuning(gr_batch* batch, int32_t* tile_size, int32_t* slice_cost,
                         int32_t* raster_waves, int32_t* bin_capacity, float* tuned_ms);
 int32_t gr_batch_destroy(gr_batch* batch);
 
@@ -263,11 +263,12 @@ int32_t gr_context_flush_l2(gr_context* ctx, int64_t bytes);
  * bins overflow is re-run by gr_draw after the bins grow. */
 int32_t gr_context_set_tuning(gr_context* ctx, int32_t tile_size, int32_t bin_capacity);
 int32_t gr_context_get_tuning(gr_context* ctx, int32_t* tile_size, int32_t* bin_capacity);
-/* Raster work split: bin entries per slice (a tile whose bin is longer is
- * shared by up to 32 CTAs) and persistent-raster waves (CTAs = SMs x resident
- * CTAs x waves); 0 keeps the current value. */
-int32_t gr_context_set_raster(gr_context* ctx, int32_t slice_entries, int32_t raster_waves);
-int32_t gr_context_get_raster(gr_context* ctx, int32_t* slice_entries, int32_t* raster_waves);
+/* Raster work split: estimated raster cost per slice (a tile's cost is the
+ * sum over its bin entries of the entry's box clipped to the tile, in pixels,
+ * plus 16; a costlier tile is shared by up to 32 CTAs) and persistent-raster
+ * waves (CTAs = SMs x resident CTAs x waves); 0 keeps the current value. */
+int32_t gr_context_set_raster(gr_context* ctx, int32_t slice_cost, int32_t raster_waves);
+int32_t gr_context_get_raster(gr_context* ctx, int32_t* slice_cost, int32_t* raster_waves);
 /* Autotunes tile size, slice length and raster waves for this frame (the
  * batch autotuner on a one-view batch) and sizes the bins; the choice stays
  * on the context. */
