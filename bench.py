@@ -431,8 +431,8 @@ def bench_present(ctx, up, scene, frames):
     p.flush()
     t0 = time.perf_counter()
     for _ in range(frames):
-        rgba, _ = p.frame(objs, cam)
-    p.flush()
+        rgba, _ = p.frame(objs, cam, copy=False)  # the host frame, valid until the next call
+    p.flush(copy=False)
     dt = time.perf_counter() - t0
     import ctypes as C
     from gorender_gb300 import _native as N

@@ -484,7 +484,9 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 // ---------------------------------------------------------------------------
 // k_project: one thread per face; everything but the general clipper.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kProjectThreads) k_project(const FrameArgs a) {
+// 4 CTAs per SM (64 registers a thread): the face pass is latency-bound, so
+// resident warps matter more than the few registers spilled.
+__global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
   __shared__ float s_S[8];
@@ -794,13 +796,16 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_bin_big: one CTA per multi-tile triangle
+// k_bin_big: one warp per multi-tile triangle
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
   const int sh = a.tile_shift;
   const int ts = 1 << sh;
   const uint32_t nbig = min(*(volatile uint32_t*)&a.work->nbig, a.big_cap);
-  for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
+  // one warp per queued triangle: most span 5 to a few dozen tiles
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nbig; q += warps) {
     const uint2 be = a.big[q];
     const uint32_t r = be.x;
     const DevView& vw = a.views[be.y];
@@ -809,7 +814,7 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
     const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
     const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
     const bool wide = (t.key & 0x80000000u) != 0;
-    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+    for (uint32_t j = lane; j < n; j += 32u) {
       const uint32_t tx = tx0 + j % nx, ty = ty0 + j / nx;
       if (!wide) {
         // conservative reject: an edge that is >= 0 over the whole

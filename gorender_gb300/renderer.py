@@ -568,23 +568,25 @@ class Presenter:
         N.check(N.lib().gr_presenter_create(renderer._h, C.byref(self._h)))
         renderer._ctx._batches.append(self)
 
-    def _take(self, ptr, tpf):
+    def _take(self, ptr, tpf, copy):
         if not ptr:
             return None, -1
         n = self.renderer.width * self.renderer.height * 4
         arr = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_uint8)), shape=(n,))
-        return arr.reshape(self.renderer.height, self.renderer.width, 4).copy(), int(tpf.value)
+        arr = arr.reshape(self.renderer.height, self.renderer.width, 4)
+        return (arr.copy() if copy else arr), int(tpf.value)
 
-    def frame(self, objects: Sequence[Object], camera: Camera):
+    def frame(self, objects: Sequence[Object], camera: Camera, copy: bool = True):
+        """copy=False returns a view of the library's page-locked buffer, valid until the next call."""
         ptr, tpf = C.c_void_p(), C.c_int64()
         N.check(N.lib().gr_presenter_frame(self._h, _c_objects(objects), len(objects), C.byref(_c_camera(camera)),
                                            C.byref(ptr), C.byref(tpf)))
-        return self._take(ptr.value, tpf)
+        return self._take(ptr.value, tpf, copy)
 
-    def flush(self):
+    def flush(self, copy: bool = True):
         ptr, tpf = C.c_void_p(), C.c_int64()
         N.check(N.lib().gr_presenter_flush(self._h, C.byref(ptr), C.byref(tpf)))
-        return self._take(ptr.value, tpf)
+        return self._take(ptr.value, tpf, copy)
 
     def close(self):
         if self._h:
