@@ -150,7 +150,7 @@ def run_ours(args):
     # tile size, raster slice and bin capacity for this frame, picked by the
     # library's autotuner (part of warm-up)
     N.check(L.gr_context_autotune(ctx.handle, up.items, n, C.byref(up.params)))
-    tuning = ctx.tuning()
+    tuning = ctx.tuning() + (ctx.raster()[0],)  # tile size, bin capacity, slice cost
     for _ in range(max(3, args.warmup)):
         gr.draw_async(ctx, up.items, n, up.params)
         ctx.flush_l2()
@@ -251,7 +251,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "faces": faces, "width": W, "height": H,
                    "binned_triangles": int(tpf.value), "parallelism": f"replicas x{ws}",
                    "l2": "flushed between frames (512 MiB write outside the timed events)",
-                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_cost": ctx.raster()[0]},
+                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_cost": tuning[2]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
                 "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
