@@ -62,6 +62,16 @@ struct TexRec {
 
 }  // namespace
 
+namespace {
+constexpr int kFrameGraphs = 4;
+struct FrameGraph {
+  cudaGraphExec_t exec = nullptr;
+  FrameArgs args{};
+  int launches = 0;
+  uint64_t used = 0;
+};
+}  // namespace
+
 struct gr_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -133,6 +143,8 @@ struct gr_context {
   size_t flush_bytes = 0;
   cudaEvent_t events[64] = {};
   int last_launches = 0;
+  FrameGraph frame_graphs[kFrameGraphs];  // captured launch sequences, by argument block
+  uint64_t frame_tick = 0;
   int32_t pending = GR_OK;
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes of the last draw
   uint32_t want_bin_cap = 0, want_rec_cap = 0, want_big_cap = 0, want_clip_cap = 0, want_ovl_cap = 0;
@@ -533,8 +545,48 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   return GR_OK;
 }
 
+// Launches a frame's kernels.  The arguments are the same from frame to frame
+// while a scene's counts and the buffers stay (items and views are read from
+// device tables), so each launch sequence is captured once into a CUDA graph
+// and replayed; a few are kept (least recently used goes first), so a caller
+// alternating between scenes replays too.
 int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr) {
   int big_blocks = 2 * 152;
+  if (!events) {
+    ++c->frame_tick;
+    int victim = 0;
+    for (int k = 0; k < kFrameGraphs; ++k) {
+      FrameGraph& fg = c->frame_graphs[k];
+      if (fg.exec && std::memcmp(&a, &fg.args, sizeof(a)) == 0) {
+        CK(cudaGraphLaunch(fg.exec, c->stream));
+        fg.used = c->frame_tick;
+        c->last_launches = fg.launches;
+        return GR_OK;
+      }
+      if (fg.used < c->frame_graphs[victim].used) victim = k;
+    }
+    FrameGraph& fg = c->frame_graphs[victim];
+    if (fg.exec) cudaGraphExecDestroy(fg.exec);
+    fg.exec = nullptr;
+    cudaGraph_t g = nullptr;
+    int n = 0;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int err = launch_frame(a, big_blocks, c->stream, &n, nullptr);
+      const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+      if (!err && e == cudaSuccess && g && cudaGraphInstantiate(&fg.exec, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        std::memcpy(&fg.args, &a, sizeof(a));
+        fg.launches = n;
+        fg.used = c->frame_tick;
+        CK(cudaGraphLaunch(fg.exec, c->stream));
+        c->last_launches = n;
+        return GR_OK;
+      }
+      if (g) cudaGraphDestroy(g);
+      fg.exec = nullptr;
+      cudaGetLastError();  // capture failed: fall back to plain launches
+    }
+  }
   int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
   return GR_OK;
@@ -602,12 +654,9 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
     Prepared pr;
     if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
     if ((st = launch(c, pr.a))) return st;
+    // the counters and the outputs in one go: one host wait per frame (a frame
+    // whose buffers overflowed is drawn again and its outputs copied again)
     CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    int32_t err;
-    int rerun = check_result(c, *c->h_result, &err);
-    if (err) return err;
-    if (rerun) continue;
     c->d2h_bytes = (int64_t)sizeof(DevResult);
     if (rgba_out && !rgba_dev) {
       CK(cudaMemcpyAsync(rgba_out, rgba, px * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -618,6 +667,10 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
       c->d2h_bytes += (int64_t)px * 4;
     }
     CK(cudaStreamSynchronize(c->stream));
+    int32_t err;
+    const int rerun = check_result(c, *c->h_result, &err);
+    if (err) return err;
+    if (rerun) continue;
     if (tpf_out) *tpf_out = (int64_t)c->h_result->tpf;
     return GR_OK;
   }
@@ -697,6 +750,8 @@ int32_t gr_context_destroy(gr_context* c) {
   if (c->flush_buf) cudaFree(c->flush_buf);
   for (auto& ev : c->events) if (ev) cudaEventDestroy(ev);
   for (auto& ev : c->stage_ev) if (ev) cudaEventDestroy(ev);
+  for (auto& fg : c->frame_graphs)
+    if (fg.exec) cudaGraphExecDestroy(fg.exec);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GR_OK;

@@ -175,3 +175,20 @@ def test_tile_sizes_and_tiny_bins(tile):
         assert c.tuning()[1] > 8
     finally:
         c.close()
+
+
+def test_alternating_scenes_replay_captured_frames(ctx):
+    """Frames are replayed from captured CUDA graphs keyed by their arguments;
+    five scenes in turn (more than the graphs kept) stay bit-exact."""
+    scs = [GOLDEN_SCENES[name]() for name in sorted(GOLDEN_SCENES)][:5]
+    ups = [gr.UploadedScene(ctx, sc) for sc in scs]
+    first = []
+    for sc, up in zip(scs, ups):
+        rgba, z, tpf = up.render()
+        ref_rgba, ref_z, ref_tpf, st = oracle.draw_scene(sc, items_override=up.matrices, nthreads=4)
+        assert st == 0 and tpf == ref_tpf and np.array_equal(rgba, ref_rgba)
+        first.append((rgba, z, tpf))
+    for _ in range(3):
+        for (rgba0, z0, tpf0), up in zip(first, ups):
+            rgba, z, tpf = up.render()
+            assert tpf == tpf0 and np.array_equal(rgba, rgba0) and np.array_equal(z.view(np.uint32), z0.view(np.uint32))
