@@ -234,7 +234,7 @@ def run_ours(args):
 
     present = bench_present(ctx, up, scene, e2e_frames)
     batched = bench_batched(ctx, args, local) if not args.skip_batched else None
-    stress = bench_stress(ctx, args) if not args.skip_batched else None
+    stress = bench_stress(local, args) if not args.skip_batched else None
     diff = bench_diff(local) if not args.skip_batched else None
 
     traffic = None
@@ -446,14 +446,17 @@ def bench_present(ctx, up, scene, frames):
             "note": "pixels only (the reference presents Pixels2); matrices built by the library per frame"}
 
 
-def bench_stress(ctx, args):
-    """The 64-icosphere 1920x1080 scene (3.6M faces, per-vertex colours):
-    device-timed frames after the autotuner, L2 flushed between frames."""
+def bench_stress(device, args):
+    """The 64-icosphere 1920x1080 scene (3.6M faces, per-vertex colours) on a
+    context of its own: device-timed frames after the autotuner, L2 flushed
+    between frames."""
     import ctypes as C
+    import gorender_gb300 as gr
     from gorender_gb300 import _native as N
     from gorender_gb300 import renderer as R
     from gorender_gb300 import scenes
 
+    ctx = gr.Context(device)
     sc = scenes.scene_icospheres_1920x1080()
     up = R.UploadedScene(ctx, sc)
     n = len(sc.objects)
@@ -471,9 +474,11 @@ def bench_stress(ctx, args):
         ctx.sync()
         t.append(ctx.elapsed_ms(4, 5))
     ms = statistics.median(t)
-    return {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
-            "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
-            "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0]}
+    out = {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
+           "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
+           "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0]}
+    ctx.close()
+    return out
 
 
 def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):

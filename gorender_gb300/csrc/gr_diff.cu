@@ -19,7 +19,10 @@
 // u and v cancel screen positions of hundreds of pixels down to a few, and on
 // thin faces D amplifies what is left, so float32 would leave relative errors
 // up to ~1e-3: hx = Q_0.p, hy = Q_1.p and W = Q_3.p are computed once per
-// (view, vertex) in double, and u, v and D per pixel in double from them.
+// (view, vertex) in double and kept as float-float pairs, and u, v and D are
+// formed per pixel in float-float arithmetic (error-free sums and products,
+// Dekker 1971; Knuth, TAOCP vol. 2) on the float32 pipes, which on this GPU
+// run about 64 times as many operations as the double-precision ones.
 // The barycentrics are homogeneous of degree 0 in D, so the clip and the
 // normalisation run in float32 on D's correctly signed values:
 //   l_i = max(s D_i, 0) / sum_j max(s D_j, 0),  s = sign(D_0 + D_1 + D_2).
@@ -41,6 +44,8 @@
 // interior term): visibility and texel choices are held fixed.
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "gr_internal.h"
 
@@ -65,14 +70,17 @@ __device__ __forceinline__ float go_max(float a, float b) {
 }
 
 // Mesh.BoundingBox (mesh.go:28-51) of pos; min and max are order-free, so a
-// tree reduction gives the sequential loop's result.  One CTA of 1024 threads.
+// tree reduction gives the sequential loop's result.  Each CTA reduces a
+// grid-strided share into partial[6 * block]; the last CTA to finish (an
+// atomic counter, no waiting) reduces the partials and writes the corners.
 __global__ void __launch_bounds__(1024) k_diff_bbox(const float* __restrict__ pos, int nv, DevItem* items,
-                                                    int num_items) {
+                                                    int num_items, float* partial, unsigned* done) {
   __shared__ float s_v[6][32];
   __shared__ float s_b[32];
+  __shared__ unsigned s_last;
   const int tid = threadIdx.x;
   float mn[3] = {pos[0], pos[1], pos[2]}, mx[3] = {pos[0], pos[1], pos[2]};
-  for (int i = tid; i < nv; i += blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + tid; i < nv; i += gridDim.x * blockDim.x) {
     const float4 p = reinterpret_cast<const float4*>(pos)[i];
     mn[0] = go_min(mn[0], p.x); mn[1] = go_min(mn[1], p.y); mn[2] = go_min(mn[2], p.z);
     mx[0] = go_max(mx[0], p.x); mx[1] = go_max(mx[1], p.y); mx[2] = go_max(mx[2], p.z);
@@ -104,6 +112,37 @@ __global__ void __launch_bounds__(1024) k_diff_bbox(const float* __restrict__ po
       }
     }
     if (lane == 0) {
+      for (int k = 0; k < 3; ++k) {
+        partial[6 * blockIdx.x + k] = mn[k];
+        partial[6 * blockIdx.x + 3 + k] = mx[k];
+      }
+      __threadfence();
+      s_last = atomicAdd(done, 1u) == gridDim.x - 1u ? 1u : 0u;
+    }
+  }
+  __syncthreads();
+  if (!s_last) return;
+  if (warp == 0) {
+    __threadfence();
+    const volatile float* pv = partial;
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = pv[k];
+      mx[k] = pv[3 + k];
+    }
+    for (unsigned b = (unsigned)lane; b < gridDim.x; b += 32) {
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = go_min(mn[k], pv[6 * b + k]);
+        mx[k] = go_max(mx[k], pv[6 * b + 3 + k]);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = go_min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+        mx[k] = go_max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+      }
+    }
+    if (lane == 0) {
+      *done = 0u;  // ready for the next forward pass
       // corners in mesh.go's order: x outermost, then y, then z; w = 1
       for (int c = 0; c < 8; ++c) {
         s_b[4 * c + 0] = (c & 4) ? mx[0] : mn[0];
@@ -144,11 +183,14 @@ __global__ void __launch_bounds__(kThreads) k_diff_vertices(const DiffArgs a) {
   const DiffView& vw = a.views[blockIdx.y];
   const float4 p = ldg4(a.pos + 4 * (size_t)i);
   const double x = p.x, y = p.y, z = p.z;
-  double* o = a.vh + 3 * ((size_t)blockIdx.y * (size_t)a.nv + (size_t)i);
+  float* o = a.vh + 6 * ((size_t)blockIdx.y * (size_t)a.nv + (size_t)i);
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const double* q = vw.Q + 4 * r;
-    o[r] = __fma_rn(q[2], z, __fma_rn(q[1], y, __fma_rn(q[0], x, q[3])));
+    const double d = __fma_rn(q[2], z, __fma_rn(q[1], y, __fma_rn(q[0], x, q[3])));
+    const float hi = (float)d;
+    o[2 * r] = hi;
+    o[2 * r + 1] = (float)(d - (double)hi);
   }
 }
 
@@ -175,6 +217,43 @@ __global__ void __launch_bounds__(kThreads) k_diff_tables(const DiffArgs a) {
   }
 }
 
+// Float-float arithmetic: a value is hi + lo with |lo| <= ulp(hi) / 2.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {  // exact: s + e = a + b
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return FF{s, e};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {  // exact when |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_sub(FF a, FF b) {
+  FF s = two_sum(a.hi, -b.hi);
+  s.lo = __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  FF s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {  // the product of the his is exact with an FMA
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fadd_rn(e, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  float e = __fmaf_rn(a.hi, b, -p);
+  e = __fadd_rn(e, __fmul_rn(a.lo, b));
+  return fast_two_sum(p, e);
+}
+
 // Geometry of one face at one pixel, shared by the forward and backward passes
 // so that both compute bit-identical values.
 struct FaceGeom {
@@ -188,32 +267,33 @@ struct FaceGeom {
 
 __device__ __forceinline__ void face_geom(const DiffArgs& a, int view, int f, int px, int py, FaceGeom& g) {
   const int* vi = a.vidx + 3 * (size_t)f;
-  const double X = (double)px, Y = (double)py;
-  double u[3], v[3];
+  const float X = (float)px, Y = (float)py;  // exact (< 2^24)
+  FF u[3], v[3];
   g.ok = true;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     g.vi[k] = __ldg(vi + k);
-    const double* h = a.vh + 3 * ((size_t)view * (size_t)a.nv + (size_t)g.vi[k]);
-    const double hx = __ldg(h), hy = __ldg(h + 1), W = __ldg(h + 2);
-    g.ok = g.ok && W < 0.0;  // in front of the camera (W is negative there)
-    u[k] = __fma_rn(-X, W, hx);
-    v[k] = __fma_rn(-Y, W, hy);
-    g.u[k] = (float)u[k];
-    g.v[k] = (float)v[k];
+    const float2* h = reinterpret_cast<const float2*>(a.vh + 6 * ((size_t)view * (size_t)a.nv + (size_t)g.vi[k]));
+    const float2 hx = __ldg(h), hy = __ldg(h + 1), w = __ldg(h + 2);
+    const FF W{w.x, w.y};
+    g.ok = g.ok && W.hi < 0.0f;  // in front of the camera (W is negative there)
+    u[k] = ff_sub(FF{hx.x, hx.y}, ff_mul_f(W, X));
+    v[k] = ff_sub(FF{hy.x, hy.y}, ff_mul_f(W, Y));
+    g.u[k] = __fadd_rn(u[k].hi, u[k].lo);
+    g.v[k] = __fadd_rn(v[k].hi, v[k].lo);
   }
-  const double D0 = __fma_rn(u[1], v[2], -(u[2] * v[1]));
-  const double D1 = __fma_rn(u[2], v[0], -(u[0] * v[2]));
-  const double D2 = __fma_rn(u[0], v[1], -(u[1] * v[0]));
-  const double T = D0 + D1 + D2;
-  g.sg = T < 0.0 ? -1.0f : 1.0f;
-  g.d[0] = g.sg * (float)D0;
-  g.d[1] = g.sg * (float)D1;
-  g.d[2] = g.sg * (float)D2;
+  const FF D0 = ff_sub(ff_mul(u[1], v[2]), ff_mul(u[2], v[1]));
+  const FF D1 = ff_sub(ff_mul(u[2], v[0]), ff_mul(u[0], v[2]));
+  const FF D2 = ff_sub(ff_mul(u[0], v[1]), ff_mul(u[1], v[0]));
+  const FF T = ff_add(ff_add(D0, D1), D2);
+  g.sg = T.hi < 0.0f ? -1.0f : 1.0f;
+  g.d[0] = g.sg * __fadd_rn(D0.hi, D0.lo);
+  g.d[1] = g.sg * __fadd_rn(D1.hi, D1.lo);
+  g.d[2] = g.sg * __fadd_rn(D2.hi, D2.lo);
 #pragma unroll
   for (int k = 0; k < 3; ++k) g.m[k] = fmaxf(g.d[k], 0.0f);
   g.M = g.m[0] + g.m[1] + g.m[2];
-  g.ok = g.ok && T != 0.0 && g.M > 0.0f && isfinite(g.M);
+  g.ok = g.ok && T.hi != 0.0f && g.M > 0.0f && isfinite(g.M);
 }
 
 struct Shade {
@@ -402,9 +482,11 @@ __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
 
 }  // namespace
 
-int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, void* stream) {
+int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, float* partial, unsigned* done,
+                     void* stream) {
   if (nv <= 0 || num_items <= 0) return 0;
-  k_diff_bbox<<<1, 1024, 0, (cudaStream_t)stream>>>(pos, nv, items, num_items);
+  const int blocks = std::min(kBBoxBlocks, (nv + 1023) / 1024);
+  k_diff_bbox<<<blocks, 1024, 0, (cudaStream_t)stream>>>(pos, nv, items, num_items, partial, done);
   return (int)cudaGetLastError();
 }
 

@@ -222,7 +222,8 @@ struct DiffArgs {
   const int* nidx;                  // nf x 3
   const float* uv;                  // nf x 6 (may be null)
   const float* nhat;                // nn x 4: normalised world-space vertex normals
-  double* vh;                       // views x nv x 3: homogeneous screen x, y and clip W
+  float* vh;                        // views x nv x 6: homogeneous screen x, y and clip W, each a
+                                    // float-float pair (hi, lo) rounded from double
   float4* col_tab;                  // per view and column x: Q_0 - x Q_3 (xyz)
   float4* row_tab;                  // per view and row y: Q_1 - y Q_3 (xyz)
   const uint32_t* ids;              // per pixel: global face index or kNoFace (raster output)
@@ -249,8 +250,11 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
 int raster_grid(int tile_shift, int waves);
 
 // Differentiable path (gr_diff.cu).
-// Writes the bounding box (Mesh.BoundingBox layout) of pos into each item's bbox.
-int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, void* stream);
+// Writes the bounding box (Mesh.BoundingBox layout) of pos into each item's
+// bbox; partial holds 6 * kBBoxBlocks floats, *done is zero between calls.
+constexpr int kBBoxBlocks = 152;
+int launch_diff_bbox(const float* pos, int nv, DevItem* items, int num_items, float* partial, unsigned* done,
+                     void* stream);
 // nhat[n] = xyz of Vec4.Normalize(world * vnrm[n]) (renderer.go:328-331), w = 0.
 int launch_diff_normals(const float* world, const float* vnrm, int nn, float* nhat, void* stream);
 // Per (view, vertex) and per (view, column / row) tables, then per pixel
