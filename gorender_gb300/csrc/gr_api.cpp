@@ -112,6 +112,9 @@ struct gr_context {
   uint32_t clip_cap = 0;
   float* vlight = nullptr;          // per-normal Gouraud intensities
   uint64_t vlight_cap = 0;
+  float4* vclip = nullptr;          // per item vertex: clip position and screen x, y (k_vertex)
+  float2* vscr = nullptr;
+  uint64_t vert_cap = 0;
   DevView* d_views = nullptr;       // view table (device) and its pinned staging
   DevView* h_views = nullptr;       // kStageSlots slots of views_cap views
   unsigned long long* view_tpf = nullptr;
@@ -433,6 +436,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   int blocks = 0;
   int light_blocks = 0;
   uint64_t light_total = 0;
+  uint64_t vert_total = 0;
+  int vert_blocks = 0;
   int live = 0;
   for (int i = 0; i < n; ++i) {
     const int m = items[i].mesh;
@@ -458,6 +463,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     d.face_base = (uint32_t)fb;
     d.block_base = blocks;
     d.view = view;
+    d.vert_base = (uint32_t)vert_total;
+    d.vert_block_base = vert_blocks;
+    vert_total += (uint64_t)mr.nv;
+    vert_blocks += (mr.nv + 255) / 256;
     blocks += (mr.nf + kProjectThreads - 1) / kProjectThreads;
     // every item gets a k_light block range (empty for non-Gouraud items) so the
     // kernel's block -> item search sees non-decreasing bases
@@ -479,6 +488,16 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
       if ((st = dev_alloc(&c->ovl, want_ovl))) return st;
       c->ovl_cap = (uint32_t)want_ovl;
     }
+  }
+  if (vert_total >= (1ull << 31)) return fail(GR_ERR_UNSUPPORTED, "more than 2^31 vertices in one frame");
+  if (vert_total > c->vert_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->vclip);
+    dev_free(c->vscr);
+    c->vert_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(vert_total, 1024);
+    if ((st = dev_alloc(&c->vclip, cap)) || (st = dev_alloc(&c->vscr, cap))) return st;
+    c->vert_cap = cap;
   }
   if (light_total > c->vlight_cap) {
     CK(cudaStreamSynchronize(c->stream));
@@ -530,6 +549,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.clip_cap = c->clip_cap;
   a.vlight = c->vlight;
   a.light_blocks = light_blocks;
+  a.vclip = c->vclip;
+  a.vscr = c->vscr;
+  a.vert_blocks = vert_blocks;
   a.work = c->work;
   a.result = c->d_result;
   a.view_tpf = c->view_tpf;
@@ -598,6 +620,7 @@ uint64_t buffers_signature(const gr_context* c) {
   const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->wide, (uintptr_t)c->tcol,
                           (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->gkey,
                           (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->big, (uintptr_t)c->vlight,
+                          (uintptr_t)c->vclip, (uintptr_t)c->vscr,
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, c->rec_cap, c->key_cap, c->bin_cap,
                           c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_cost,
@@ -740,6 +763,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
+  dev_free(c->vclip); dev_free(c->vscr);
   dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan);
   dev_free(c->ovl); dev_free(c->ovl_key);
   if (c->h_views) cudaFreeHost(c->h_views);

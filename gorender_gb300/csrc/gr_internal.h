@@ -70,6 +70,8 @@ struct DevItem {
   int light_base;                   // first entry of this item in FrameArgs::vlight
   int light_block_base;             // first k_light block of this item
   int view;                         // index into FrameArgs::views
+  uint32_t vert_base;               // first entry of this item in FrameArgs::vclip / vscr
+  int vert_block_base;              // first k_vertex block of this item
 };
 
 // Raster setup of one binned triangle (64 bytes).  For "narrow" triangles
@@ -169,6 +171,9 @@ struct FrameArgs {
   uint32_t clip_cap;
   float* vlight;                    // per-normal Gouraud intensities (k_light)
   int light_blocks;                 // k_light grid (0: no Gouraud item)
+  float4* vclip;                    // per item vertex: clip-space position (k_vertex)
+  float2* vscr;                     // per item vertex: screen x, y before int() (k_vertex)
+  int vert_blocks;                  // k_vertex grid
   unsigned long long* gkey;         // tiles x 1024 merged visibility keys of split tiles (zero when idle)
   uint32_t* tile_done;              // per tile: slices finished (zero when idle)
   uint32_t slice_cost;              // raster cost per slice (k_plan splits costlier tiles)

@@ -164,15 +164,40 @@ struct SV {
   float sx, sy, W, u, v, in, r, g, b;
 };
 
-__device__ __forceinline__ SV to_screen(const PV& q, const float* S) {
-  float W = q.p.w;
-  float dx = fd(q.p.x, W), dy = fd(q.p.y, W), dz = fd(q.p.z, W), dw = fd(q.p.w, W);
+// Divide + screen map of a clip-space position (renderer.go:361-370): the
+// whole vector divided by W (so W/W = 1), then the screen matrix's rows 0, 1.
+__device__ __forceinline__ float2 screen_of(V4 p, const float* S) {
+  const float W = p.w;
+  const float dx = fd(p.x, W), dy = fd(p.y, W), dz = fd(p.z, W), dw = fd(p.w, W);
+  return make_float2(fa(fa(fa(fm(S[0], dx), fm(S[1], dy)), fm(S[2], dz)), fm(S[3], dw)),
+                     fa(fa(fa(fm(S[4], dx), fm(S[5], dy)), fm(S[6], dz)), fm(S[7], dw)));
+}
+
+// Screen vertex from precomputed screen coordinates and the corner's attributes.
+__device__ __forceinline__ SV sv_of(float2 scr, float W, const PV& q) {
   SV s;
-  s.sx = fa(fa(fa(fm(S[0], dx), fm(S[1], dy)), fm(S[2], dz)), fm(S[3], dw));
-  s.sy = fa(fa(fa(fm(S[4], dx), fm(S[5], dy)), fm(S[6], dz)), fm(S[7], dw));
+  s.sx = scr.x;
+  s.sy = scr.y;
   s.X = go_int(s.sx);
   s.Y = go_int(s.sy);
   s.W = W;
+  s.u = q.u;
+  s.v = q.v;
+  s.in = q.in;
+  s.r = q.r;
+  s.g = q.g;
+  s.b = q.b;
+  return s;
+}
+
+__device__ __forceinline__ SV to_screen(const PV& q, const float* S) {
+  const float2 scr = screen_of(q.p, S);
+  SV s;
+  s.sx = scr.x;
+  s.sy = scr.y;
+  s.X = go_int(s.sx);
+  s.Y = go_int(s.sy);
+  s.W = q.p.w;
   s.u = q.u;
   s.v = q.v;
   s.in = q.in;
@@ -452,14 +477,41 @@ __device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const
 }
 
 // Block -> item: the last item whose first block is <= blockIdx.x.
-__device__ __forceinline__ int find_item(const FrameArgs& a, bool light_blocks) {
+// The item owning this block: kind 0 face blocks (k_project), 1 normal blocks
+// (k_light), 2 vertex blocks (k_vertex); the bases never decrease.
+__device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
   int lo = 0, hi = a.num_items - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    int base = light_blocks ? a.items[mid].light_block_base : a.items[mid].block_base;
+    const DevItem& m = a.items[mid];
+    int base = kind == 1 ? m.light_block_base : kind == 2 ? m.vert_block_base : m.block_base;
     if (base <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
   }
   return lo;
+}
+
+// ---------------------------------------------------------------------------
+// k_vertex: every vertex of every item transformed once per frame
+// (matrixMultiplyVec4Batch, renderer.go:303-304) and mapped to the screen
+// (renderer.go:361-370).  Faces share vertices, and the result of a vertex
+// does not depend on the face that uses it, so the face pass gathers these
+// instead of transforming each corner again.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
+  __shared__ float s_mvp[16];
+  __shared__ float s_S[8];
+  __shared__ int s_item;
+  if (threadIdx.x == 0) s_item = find_item(a, 2);
+  __syncthreads();
+  const DevItem& it = a.items[s_item];
+  if (threadIdx.x < 16) s_mvp[threadIdx.x] = it.mvp[threadIdx.x];
+  if (threadIdx.x < 8) s_S[threadIdx.x] = a.views[it.view].S[threadIdx.x];
+  __syncthreads();
+  const int v = ((int)blockIdx.x - it.vert_block_base) * 256 + (int)threadIdx.x;
+  if (v >= it.nv) return;
+  const V4 c = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)v));
+  a.vclip[it.vert_base + v] = make_float4(c.x, c.y, c.z, c.w);
+  a.vscr[it.vert_base + v] = screen_of(c, s_S);
 }
 
 // ---------------------------------------------------------------------------
@@ -471,7 +523,7 @@ __device__ __forceinline__ int find_item(const FrameArgs& a, bool light_blocks) 
 __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
   __shared__ float s_world[16];
   __shared__ int s_item;
-  if (threadIdx.x == 0) s_item = find_item(a, true);
+  if (threadIdx.x == 0) s_item = find_item(a, 1);
   __syncthreads();
   const DevItem& it = a.items[s_item];
   if (threadIdx.x < 16) s_world[threadIdx.x] = it.world[threadIdx.x];
@@ -489,13 +541,12 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
-  __shared__ float s_S[8];
   __shared__ int s_item;
   __shared__ int s_vis;
   __shared__ unsigned s_out[8];
 
   const int tid = threadIdx.x;
-  if (tid == 0) s_item = find_item(a, false);
+  if (tid == 0) s_item = find_item(a, 0);
   __syncthreads();
   const int item = s_item;
   const DevItem& it = a.items[item];
@@ -504,7 +555,6 @@ __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs 
     s_mvp[tid] = it.mvp[tid];
     s_world[tid] = it.world[tid];
   }
-  if (tid < 8) s_S[tid] = vw.S[tid];
   __syncthreads();
   // Frustum.BoxVisibility of the transformed bounding box (renderer.go:268-275).
   if (tid < 8) {
@@ -544,9 +594,10 @@ __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs 
   SV s0, s1, s2;
   if (valid) {
     const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
-    const V4 v0 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i0));
-    const V4 v1 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i1));
-    const V4 v2 = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)i2));
+    // clip-space corners from k_vertex (the same arithmetic, done once per vertex)
+    const float4 c0 = __ldg(a.vclip + it.vert_base + i0), c1 = __ldg(a.vclip + it.vert_base + i1),
+                 c2 = __ldg(a.vclip + it.vert_base + i2);
+    const V4 v0{c0.x, c0.y, c0.z, c0.w}, v1{c1.x, c1.y, c1.z, c1.w}, v2{c2.x, c2.y, c2.z, c2.w};
     bool draw = !(fl & 0x04u) || facing_camera(v0, v1, v2);  // BackfaceCulling
     // Frustum clipping (renderer.go:349-359).  At the first plane, in clipping
     // order, where not all three vertices are inside: all outside means the
@@ -565,11 +616,10 @@ __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs 
     }
     if (draw && !general) {
       PV p0, p1, p2;
-      p0.p = v0; p1.p = v1; p2.p = v2;
       face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
-      s0 = to_screen(p0, s_S);
-      s1 = to_screen(p1, s_S);
-      s2 = to_screen(p2, s_S);
+      s0 = sv_of(__ldg(a.vscr + it.vert_base + i0), v0.w, p0);
+      s1 = sv_of(__ldg(a.vscr + it.vert_base + i1), v1.w, p1);
+      s2 = sv_of(__ldg(a.vscr + it.vert_base + i2), v2.w, p2);
       if (bin_test(s0, s1, s2, (float)W, (float)H)) {
         ntpf = 1;
         Setup s;
@@ -1587,6 +1637,8 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
       k_light<<<a.light_blocks, 256, 0, s>>>(a);
       ++n;
     }
+    k_vertex<<<a.vert_blocks, 256, 0, s>>>(a);
+    ++n;
     k_project<<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);

@@ -13,7 +13,8 @@
 //
 // Limits (larger frames are rejected with GR_ERR_UNSUPPORTED): at most
 // kMaxFaces faces per frame, kMaxObjects objects, kMaxTextures textures,
-// kMaxNormals vertex normals across Gouraud-lit objects, and a framebuffer of
+// kMaxNormals vertex normals across Gouraud-lit objects, kMaxVertices vertex
+// positions across objects, and a framebuffer of
 // at most kMaxSide x kMaxSide pixels.  Bins and record buffers cannot grow
 // here: a frame that would overflow them returns GR_ERR_BIN_OVERFLOW.
 //
@@ -41,6 +42,7 @@ constexpr int kMaxFaces = 4096;
 constexpr int kMaxObjects = 16;
 constexpr int kMaxTextures = 16;
 constexpr int kMaxNormals = 16384;
+constexpr int kMaxVertices = 32768;
 constexpr int kMaxSide = 512;
 constexpr int kTiles = (kMaxSide / 32) * (kMaxSide / 32);
 constexpr uint32_t kRecCap = 3u * kMaxFaces;
@@ -56,7 +58,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
   size_t items, texs, views, view_tpf, view_tpf_out, plan, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip,
-      vlight, gkey, tile_done, work, result, end;
+      vlight, vclip, vscr, gkey, tile_done, work, result, end;
 };
 
 constexpr Layout make_layout() {
@@ -79,6 +81,8 @@ constexpr Layout make_layout() {
   l.big = o; o += up256(sizeof(uint2) * kQueueCap);
   l.clip = o; o += up256(sizeof(uint2) * kQueueCap);
   l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
+  l.vclip = o; o += up256(sizeof(float4) * kMaxVertices);
+  l.vscr = o; o += up256(sizeof(float2) * kMaxVertices);
   l.gkey = o; o += up256(sizeof(unsigned long long) * kTiles * 1024);
   l.tile_done = o; o += up256(sizeof(uint32_t) * kTiles);
   l.work = o; o += up256(sizeof(DevWork));
@@ -116,7 +120,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
     return set_error(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
   const bool gouraud_frame = (p->flags & GR_LIGHTING) && !(p->flags & GR_FLAT_SHADING);
-  long faces = 0, normals = 0;
+  long faces = 0, normals = 0, vertices = 0;
   for (int i = 0; i < num_objects; ++i) {
     const gr_mesh_desc& m = objects[i].mesh;
     if (m.num_faces < 0 || m.num_vertices <= 0 || !m.positions || (m.num_faces > 0 && (!m.vertex_indices || !m.face_normals)))
@@ -124,10 +128,13 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     if (gouraud_frame && m.num_normals > 0 && (!m.vertex_normals || !m.normal_indices))
       return set_error(GR_ERR_BAD_INDEX, "gr_draw_noalloc: object %d has vertex normals without normal indices", i);
     faces += m.num_faces;
+    if (m.num_faces > 0) vertices += m.num_vertices;
     if (gouraud_frame) normals += m.num_normals;
   }
   if (faces > kMaxFaces)
     return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld faces exceed the limit of %d", faces, kMaxFaces);
+  if (vertices > kMaxVertices)
+    return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld vertices exceed the limit of %d", vertices, kMaxVertices);
   if (normals > kMaxNormals)
     return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld vertex normals exceed the limit of %d", normals,
                      kMaxNormals);
@@ -155,7 +162,8 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   DevTex texs[kMaxTextures];
   std::memset(items, 0, sizeof(items));
   std::memset(texs, 0, sizeof(texs));
-  int live = 0, blocks = 0, light_blocks = 0, light_total = 0;
+  int live = 0, blocks = 0, light_blocks = 0, light_total = 0, vert_blocks = 0;
+  uint32_t vert_total = 0;
   uint32_t face_base = 0;
   for (int i = 0; i < num_objects; ++i) {
     const gr_mesh_desc& m = objects[i].mesh;
@@ -173,6 +181,10 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     d.block_base = blocks;
     d.view = 0;
     blocks += (m.num_faces + kProjectThreads - 1) / kProjectThreads;
+    d.vert_base = vert_total;
+    d.vert_block_base = vert_blocks;
+    vert_total += (uint32_t)m.num_vertices;
+    vert_blocks += (m.num_vertices + 255) / 256;
     d.light_base = light_total;
     d.light_block_base = light_blocks;
     if (gouraud_frame && d.nn > 0) {
@@ -247,6 +259,9 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.big = (uint2*)(base + kLayout.big);
   a.clip = (uint2*)(base + kLayout.clip);
   a.vlight = (float*)(base + kLayout.vlight);
+  a.vclip = (float4*)(base + kLayout.vclip);
+  a.vscr = (float2*)(base + kLayout.vscr);
+  a.vert_blocks = vert_blocks;
   a.gkey = (unsigned long long*)(base + kLayout.gkey);
   a.tile_done = (uint32_t*)(base + kLayout.tile_done);
   a.work = (DevWork*)(base + kLayout.work);
