@@ -1000,24 +1000,93 @@ struct RasterShape {
 // the depth the pixel already holds, with a 1e-5 margin for the roundings,
 // loses strictly (ties, where draw order decides, are never skipped), so its
 // five divisions are not needed.
+// The depth test proper at pixel p with edge values e12, e20 (as floats).
+__device__ __forceinline__ void depth_at(unsigned long long* p, const TriRaster& t, float e12f, float e20f) {
+  float al, be, ga;
+  const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
+  if (!(z >= -1.0f)) return;  // rasterizer.go:156 against the cleared Z of -1
+  const unsigned long long k = depth_key(z, t.key);
+  if (k > *(volatile unsigned long long*)p) atomicMax(p, k);
+}
+
+// True when the pixel at p already holds a depth that a candidate with
+// vertex depths w0..w2 cannot reach (the early out above).
+__device__ __forceinline__ bool depth_beaten(const unsigned long long* p, const TriRaster& t) {
+  const uint32_t o = (uint32_t)(*(const volatile unsigned long long*)p >> 32);
+  if (!(o & 0x80000000u)) return false;  // the pixel holds a depth < +0
+  const float wmin = fminf(fminf(-t.w0, -t.w1), -t.w2);
+  return wmin > 0.0f && __fmul_rn(__uint_as_float(o & 0x7FFFFFFFu), wmin) > 1.00001f;
+}
+
 template <int TS>
 __device__ __forceinline__ void depth_candidate(unsigned long long* skey, const TriRaster& t, const TriWide* wide,
                                                 uint32_t r, int x, int y, int tx0, int ty0) {
   unsigned long long* p = skey + (y - ty0) * RasterShape<TS>::kStride + (x - tx0);
-  const unsigned long long cur = *(volatile unsigned long long*)p;
-  const uint32_t o = (uint32_t)(cur >> 32);
-  if (o & 0x80000000u) {  // the pixel holds a depth >= +0
-    const float wmin = fminf(fminf(-t.w0, -t.w1), -t.w2);
-    if (wmin > 0.0f && __fmul_rn(__uint_as_float(o & 0x7FFFFFFFu), wmin) > 1.00001f) return;
-  }
+  if (depth_beaten(p, t)) return;
   bool inside;
   float e12f, e20f;
   edges_at(t, wide, r, x, y, inside, e12f, e20f);
-  float al, be, ga;
-  float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
-  if (!(z >= -1.0f)) return;  // rasterizer.go:156 against the cleared Z of -1
-  unsigned long long k = depth_key(z, t.key);
-  if (k > *(volatile unsigned long long*)p) atomicMax(p, k);
+  depth_at(p, t, e12f, e20f);
+}
+
+// Depth test of a pixel known to be covered by narrow triangle t.
+template <int TS>
+__device__ __forceinline__ void depth_covered(unsigned long long* skey, const TriRaster& t, int x, int y, int tx0,
+                                              int ty0) {
+  unsigned long long* p = skey + (y - ty0) * RasterShape<TS>::kStride + (x - tx0);
+  if (depth_beaten(p, t)) return;
+  const int e12 = t.a12 * x + t.b12 * y + t.c12;
+  const int e20 = t.a20 * x + t.b20 * y + t.c20;
+  depth_at(p, t, __int2float_rn(e12), __int2float_rn(e20));
+}
+
+// floor(n / d) for d > 0, exact when the quotient lies in [lo - 1, hi + 1];
+// otherwise a value on the same side of that range.  The float estimate is
+// within one of the quotient (|n| < 2^31, d < 2^15: a few ulps of relative
+// error, below 1 while |n / d| < 2^20; beyond that the clamp decides), and
+// one exact integer step corrects it.
+__device__ __forceinline__ int floor_div_near(int n, int d, int lo, int hi) {
+  float q = floorf(__fdividef(__int2float_rn(n), __int2float_rn(d)));
+  q = fminf(fmaxf(q, (float)(lo - 1)), (float)(hi + 1));
+  int qi = (int)q;
+  if (qi * d > n) --qi;
+  else if ((qi + 1) * d <= n) ++qi;
+  return qi;
+}
+
+// Narrows [xl, xr] on row y to the x where a*x + (b*y + c) < 0 (one edge of
+// the inside test, rasterizer.go:147).  All products stay in int32 for
+// narrow triangles (|a|, |b| < 2^15, |c| < 2^29, 0 <= x, y < 2^14).
+__device__ __forceinline__ void span_edge(int a, int b, int c, int y, int& xl, int& xr) {
+  const int k = b * y + c;
+  const int n = a > 0 ? -k - 1 : k;  // a > 0: x <= floor((-k-1)/a); a < 0: x >= floor(k/-a) + 1
+  const int q = floor_div_near(n, a > 0 ? a : max(-a, 1), xl, xr);
+  if (a > 0) xr = min(xr, q);
+  else if (a < 0) xl = max(xl, q + 1);
+  else if (k >= 0) xr = xl - 1;      // a == 0: the whole row is outside this edge
+}
+
+// Last lane j with start[j] <= g (start non-decreasing across lanes, lane 0's
+// start <= g); zero-length lanes share the next lane's start and are skipped.
+__device__ __forceinline__ int owner_lane(int start, int g) {
+  int own = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1) {
+    const int cand = own + step;
+    const int cs = __shfl_sync(FULL_MASK, start, cand & 31);
+    if (cand < 32 && cs <= g) own = cand;
+  }
+  return own;
+}
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULL_MASK, v, o);
+    if ((int)lane >= o) v += y;
+  }
+  return v;
 }
 
 // Coverage test of one pixel (rasterizer.go:147).
@@ -1179,13 +1248,13 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   uint32_t* trec = s_trec[warp];
   CandQueue<TS> q{s_ent[warp], tri, trec, 0};
   // Entries per warp chunk: small bins use shorter chunks so that every warp
-  // gets some (the coverage walk below keeps all lanes busy either way).
+  // gets some (the span walk below keeps all lanes busy either way).
   const uint32_t chunk = min(32u, max(8u, (hi - lo + 2u * kWarps - 1u) / (2u * kWarps)));
   for (;;) {
     // Phase 1: warps take `chunk` bin entries at a time from a shared cursor.
-    // Footprints up to kLaneArea pixels run one lane per triangle in a
-    // converged loop (so covered pixels can be queued warp-synchronously);
-    // larger or int64 triangles are queued for the whole CTA.
+    // Narrow triangles with footprints up to kLaneArea pixels are walked by
+    // the warp that took them (span walk below); larger or int64 triangles
+    // are queued for the whole CTA.
     for (;;) {
       if (*(volatile uint32_t*)&s_nlarge >= kLargeCap) break;
       uint32_t b = 0;
@@ -1219,62 +1288,61 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
         tri[lane] = t;
         trec[lane] = r;
       }
-      // Flattened coverage walk: the chunk's (triangle, footprint pixel)
-      // pairs are numbered consecutively (a warp scan of the footprint
-      // areas) and each iteration tests 32 of them, so the warp runs
-      // ceil(total / 32) iterations rather than the largest footprint.
-      const int my = by_lane ? area : 0;
-      int incl = my;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL_MASK, incl, o);
-        if ((int)lane >= o) incl += y;
-      }
+      // Span walk.  The chunk's (triangle, footprint row) pairs are numbered
+      // consecutively (a warp scan of the row counts), 32 rows per step; each
+      // lane narrows its row to the exact covered x-range, and the covered
+      // pixels of the 32 spans are numbered again and depth-tested 32 at a
+      // time, so no lane tests a pixel that the triangle does not cover.
+      // Chunks of tiny footprints take the per-lane box walk instead.
+      const int my = by_lane ? ly1 - ly0 + 1 : 0;
+      const int incl = warp_incl_scan(my);
       const int excl = incl - my;
       const int total = __shfl_sync(FULL_MASK, incl, 31);
-      const int bw = lx1 - lx0 + 1;                       // footprint width, <= TS
-      const int magic = by_lane ? (65536 + bw - 1) / bw : 0;  // exact o / bw for o < 2048
+      const int widest = __reduce_max_sync(FULL_MASK, by_lane ? area : 0);
       __syncwarp();
-      const int widest = __reduce_max_sync(FULL_MASK, my);
-      if (((total + 31) >> 5) * 9 >= widest * 5) {
-        // footprints of similar size: one lane per triangle is cheaper
+      if (widest * 5 <= ((total + 31) >> 5) * 27) {
+        // Footprints of a few pixels: a span costs about five box-pixel tests,
+        // so each lane tests its own box, queueing covered pixels.
         int x = lx0, y = ly0;
         for (int it = 0; it < widest; ++it) {
-          const bool c = it < my && t.a01 * x + t.b01 * y + t.c01 < 0 && t.a12 * x + t.b12 * y + t.c12 < 0 &&
-                         t.a20 * x + t.b20 * y + t.c20 < 0;
+          const bool c = by_lane && it < area && t.a01 * x + t.b01 * y + t.c01 < 0 &&
+                         t.a12 * x + t.b12 * y + t.c12 < 0 && t.a20 * x + t.b20 * y + t.c20 < 0;
           q.push(c, lane, x - tx0, y - ty0, skey, a, tx0, ty0);
           if (++x > lx1) {
             x = lx0;
             ++y;
           }
         }
-      } else
+        q.flush(skey, a, tx0, ty0);
+        continue;
+      }
       for (int g0 = 0; g0 < total; g0 += 32) {
         const int g = g0 + (int)lane;
-        // owner: the last lane whose range starts at or before g (zero-area
-        // lanes share the next lane's start and are never chosen)
-        int own = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          const int cand = own + step;
-          const int ce = __shfl_sync(FULL_MASK, excl, cand & 31);
-          if (cand < 32 && ce <= g) own = cand;
-        }
-        const int o = g - __shfl_sync(FULL_MASK, excl, own);
-        const int ow = __shfl_sync(FULL_MASK, bw, own);
-        const int om = __shfl_sync(FULL_MASK, magic, own);
-        const int ox = __shfl_sync(FULL_MASK, lx0, own), oy = __shfl_sync(FULL_MASK, ly0, own);
-        const int dy = (o * om) >> 16;
-        const int x = ox + (o - dy * ow), y = oy + dy;
-        bool c = false;
+        const int own = owner_lane(excl, g);
+        const int y = __shfl_sync(FULL_MASK, ly0, own) + g - __shfl_sync(FULL_MASK, excl, own);
+        int xl = __shfl_sync(FULL_MASK, lx0, own), xr = __shfl_sync(FULL_MASK, lx1, own);
         if (g < total) {
           const TriRaster& tt = tri[own];
-          c = tt.a01 * x + tt.b01 * y + tt.c01 < 0 && tt.a12 * x + tt.b12 * y + tt.c12 < 0 &&
-              tt.a20 * x + tt.b20 * y + tt.c20 < 0;
+          span_edge(tt.a01, tt.b01, tt.c01, y, xl, xr);
+          span_edge(tt.a12, tt.b12, tt.c12, y, xl, xr);
+          span_edge(tt.a20, tt.b20, tt.c20, y, xl, xr);
+        } else {
+          xr = xl - 1;
         }
-        q.push(c, (uint32_t)own, x - tx0, y - ty0, skey, a, tx0, ty0);
+        const int len = max(xr - xl + 1, 0);
+        const int incl2 = warp_incl_scan(len);
+        const int excl2 = incl2 - len;
+        const int total2 = __shfl_sync(FULL_MASK, incl2, 31);
+        for (int h0 = 0; h0 < total2; h0 += 32) {
+          const int h = h0 + (int)lane;
+          const int o2 = owner_lane(excl2, h);
+          const int x = __shfl_sync(FULL_MASK, xl, o2) + h - __shfl_sync(FULL_MASK, excl2, o2);
+          const int yy = __shfl_sync(FULL_MASK, y, o2);
+          const int slot = __shfl_sync(FULL_MASK, own, o2);
+          if (h < total2) depth_covered<TS>(skey, tri[slot], x, yy, tx0, ty0);
+        }
       }
-      q.flush(skey, a, tx0, ty0);  // lane slots are rewritten by the next chunk
+      __syncwarp();  // lane slots are rewritten by the next chunk
     }
     __syncthreads();
     const uint32_t nl = s_nlarge;
