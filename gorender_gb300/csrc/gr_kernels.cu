@@ -1192,8 +1192,8 @@ __device__ __forceinline__ uint32_t tile_slices(const FrameArgs& a, uint32_t n, 
 template <int TS>
 struct RasterSmem {
   static constexpr int kWarps = RasterShape<TS>::kWarps;
-  static constexpr uint32_t kLargeCap = 128;  // queued large triangles per round
-  static constexpr int kSlots = 64;           // triangle table: 32 lane slots + 32 for large ones
+  static constexpr uint32_t kLargeCap = 128;  // queued wide triangles per round
+  static constexpr int kSlots = 64;           // triangle table: 32 lane slots + 32 for wide ones
   __align__(16) unsigned long long skey[TS * RasterShape<TS>::kStride];
   __align__(16) TriRaster tri[kWarps][kSlots];
   uint32_t trec[kWarps][kSlots];
@@ -1210,7 +1210,6 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   constexpr int kStride = RasterShape<TS>::kStride;
   constexpr int kWarps = RasterShape<TS>::kWarps;
   constexpr uint32_t kLargeCap = RasterSmem<TS>::kLargeCap;
-  constexpr int kLaneArea = 256;          // footprints up to 256 pixels: one lane each
   unsigned long long* skey = sm.skey;
   auto& s_tri = sm.tri;
   auto& s_trec = sm.trec;
@@ -1252,9 +1251,8 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   const uint32_t chunk = min(32u, max(8u, (hi - lo + 2u * kWarps - 1u) / (2u * kWarps)));
   for (;;) {
     // Phase 1: warps take `chunk` bin entries at a time from a shared cursor.
-    // Narrow triangles with footprints up to kLaneArea pixels are walked by
-    // the warp that took them (span walk below); larger or int64 triangles
-    // are queued for the whole CTA.
+    // Narrow triangles are walked by the warp that took them (span walk
+    // below); int64 ("wide") triangles are queued for the whole CTA.
     for (;;) {
       if (*(volatile uint32_t*)&s_nlarge >= kLargeCap) break;
       uint32_t b = 0;
@@ -1274,7 +1272,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       }
       const bool live = valid && lx1 >= lx0 && ly1 >= ly0;
       const int area = live ? (lx1 - lx0 + 1) * (ly1 - ly0 + 1) : 0;
-      const bool by_lane = live && area <= kLaneArea && !(t.key & 0x80000000u);
+      const bool by_lane = live && !(t.key & 0x80000000u);
       const bool large = live && !by_lane;
       const unsigned lm = __ballot_sync(FULL_MASK, large);
       if (lm) {
@@ -1347,14 +1345,14 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     __syncthreads();
     const uint32_t nl = s_nlarge;
     const bool more = s_next < hi;
-    // Phase 2: every warp walks the queued large triangles and takes an
+    // Phase 2: every warp walks the queued wide triangles and takes an
     // interleaved share of their 8x4 blocks (global block index mod warps).
     int base = 0;
     for (uint32_t k = 0; k < nl; ++k) {
       const uint32_t slot = 32u + (k & 31u);
       if ((k & 31u) == 0) {
         // slots 32..63 are about to be reused: drain, then stage the next 32
-        // large records with one load per lane
+        // wide records with one load per lane
         q.flush(skey, a, tx0, ty0);
         if (k + lane < nl) {
           const uint32_t r2 = s_large[k + lane];
