@@ -573,7 +573,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
 // and replayed; a few are kept (least recently used goes first), so a caller
 // alternating between scenes replays too.
 int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr) {
-  int big_blocks = 2 * 152;
+  int big_blocks = kBigBlocks;
   if (!events) {
     ++c->frame_tick;
     int victim = 0;
@@ -1039,7 +1039,7 @@ int32_t batch_capture(gr_batch* b) {
   if (st) return st;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  int err = launch_frame(pr.a, 2 * 152, c->stream, &b->launches, nullptr);
+  int err = launch_frame(pr.a, kBigBlocks, c->stream, &b->launches, nullptr);
   cudaError_t e2 = cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream);
   cudaError_t e3 = cudaMemcpyAsync(c->h_view_tpf, c->view_tpf_out, sizeof(unsigned long long) * nv,
                                    cudaMemcpyDeviceToHost, c->stream);

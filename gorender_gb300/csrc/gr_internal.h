@@ -22,6 +22,7 @@ constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a 
 constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
+constexpr int kBigBlocks = 3 * 152;           // k_bin_big / k_overlay grid (grid-stride over the queue)
 
 // Texture table entry (texture.go:19-26).
 struct DevTex {

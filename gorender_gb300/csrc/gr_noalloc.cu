@@ -285,7 +285,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   if (e == cudaSuccess && num_textures)
     e = cudaMemcpyAsync(base + kLayout.texs, texs, sizeof(DevTex) * num_textures, cudaMemcpyHostToDevice, s);
   int launches = 0;
-  if (e == cudaSuccess) e = (cudaError_t)launch_frame(a, 2 * 152, s, &launches, nullptr);
+  if (e == cudaSuccess) e = (cudaError_t)launch_frame(a, kBigBlocks, s, &launches, nullptr);
   DevResult r;
   std::memset(&r, 0, sizeof(r));
   if (e == cudaSuccess) e = cudaMemcpyAsync(&r, base + kLayout.result, sizeof(r), cudaMemcpyDeviceToHost, s);
