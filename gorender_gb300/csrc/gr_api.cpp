@@ -129,6 +129,8 @@ struct gr_context {
   Overlay* ovl = nullptr;           // ShowEdges / ShowVertices marks
   uint32_t ovl_cap = 0;
   uint32_t* ovl_key = nullptr;      // per pixel of all views (zero when idle)
+  unsigned long long* pkey = nullptr;  // per pixel of all views: keys for k_resolve
+  uint64_t pkey_pixels = 0;
   uint64_t ovl_pixels = 0;
   int raster_waves = 1;             // persistent raster CTAs = SMs x resident CTAs x waves
   int last_views = 0;               // views of the last batched draw
@@ -175,6 +177,18 @@ bool is_device_ptr(const void* p) {
     return false;
   }
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Device address of page-locked host memory (null for any other pointer):
+// the kernels write a frame's outputs there directly, with no copy after it.
+void* mapped_host_ptr(void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
 template <class T>
@@ -403,6 +417,17 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     CK(cudaMemsetAsync(c->ovl_key, 0, sizeof(uint32_t) * total_pixels, c->stream));
     c->ovl_pixels = total_pixels;
   }
+  // One view: k_raster stores the final keys and k_resolve shades every
+  // pixel at full occupancy.  Many views: k_raster shades each tile (the
+  // keys of a large batch would cost more memory traffic than they save).
+  const bool separate = nviews == 1;
+  if (separate && total_pixels > c->pkey_pixels) {
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->pkey);
+    c->pkey_pixels = 0;
+    if ((st = dev_alloc(&c->pkey, (size_t)total_pixels))) return st;
+    c->pkey_pixels = total_pixels;
+  }
   const int slot = (c->stage_slot + 1) % kStageSlots;
   if (c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
   DevView* hviews = c->h_views + (size_t)slot * c->views_cap;
@@ -562,6 +587,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.ovl = c->ovl;
   a.ovl_cap = c->ovl_cap;
   a.ovl_key = c->ovl_key;
+  a.pkey = separate ? c->pkey : nullptr;
+  a.total_pixels = total_pixels;
   out.faces = faces;
   out.nitems = live;
   return GR_OK;
@@ -624,7 +651,7 @@ uint64_t buffers_signature(const gr_context* c) {
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, c->rec_cap, c->key_cap, c->bin_cap,
                           c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_cost,
-                          (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key,
+                          (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key, (uintptr_t)c->pkey,
                           c->ovl_cap};
   uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
   for (uintptr_t v : ps) {
@@ -663,10 +690,14 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
   if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "params is NULL");
   const size_t px = (size_t)p->width * (size_t)p->height;
   const bool rgba_dev = is_device_ptr(rgba_out), z_dev = is_device_ptr(z_out);
+  // page-locked host outputs are written by the kernels through their device
+  // addresses; pageable ones are copied from the context's framebuffer
+  uint32_t* rgba_map = rgba_dev ? nullptr : (uint32_t*)mapped_host_ptr(rgba_out);
+  float* z_map = z_dev ? nullptr : (float*)mapped_host_ptr(z_out);
   int32_t st;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    uint32_t* rgba = rgba_dev ? (uint32_t*)rgba_out : nullptr;
-    float* z = z_dev ? z_out : nullptr;
+    uint32_t* rgba = rgba_dev ? (uint32_t*)rgba_out : rgba_map;
+    float* z = z_dev ? z_out : z_map;
     if (!rgba || !z) {
       if (p->width <= 0 || p->height <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad framebuffer size");
       if ((st = ensure_fb(c, px))) return st;
@@ -682,11 +713,11 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
     CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
     c->d2h_bytes = (int64_t)sizeof(DevResult);
     if (rgba_out && !rgba_dev) {
-      CK(cudaMemcpyAsync(rgba_out, rgba, px * 4, cudaMemcpyDeviceToHost, c->stream));
+      if (!rgba_map) CK(cudaMemcpyAsync(rgba_out, rgba, px * 4, cudaMemcpyDeviceToHost, c->stream));
       c->d2h_bytes += (int64_t)px * 4;
     }
     if (z_out && !z_dev) {
-      CK(cudaMemcpyAsync(z_out, z, px * 4, cudaMemcpyDeviceToHost, c->stream));
+      if (!z_map) CK(cudaMemcpyAsync(z_out, z, px * 4, cudaMemcpyDeviceToHost, c->stream));
       c->d2h_bytes += (int64_t)px * 4;
     }
     CK(cudaStreamSynchronize(c->stream));
@@ -765,7 +796,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);
   dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan);
-  dev_free(c->ovl); dev_free(c->ovl_key);
+  dev_free(c->ovl); dev_free(c->ovl_key); dev_free(c->pkey);
   if (c->h_views) cudaFreeHost(c->h_views);
   if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
   dev_free(c->work); dev_free(c->d_result);

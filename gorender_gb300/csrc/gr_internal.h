@@ -188,6 +188,9 @@ struct FrameArgs {
   Overlay* ovl;                     // overlay records (views with ShowEdges / ShowVertices)
   uint32_t ovl_cap;
   uint32_t* ovl_key;                // per pixel of every view: max (order key * 2 + vertex mark), 0 = none
+  unsigned long long* pkey;         // per pixel of every view: final visibility keys, shaded by k_resolve
+                                    // (null: k_raster shades each tile itself)
+  unsigned long long total_pixels;  // sum of the views' pixels
 };
 
 // View flag (internal, never set by callers): the raster resolve writes the

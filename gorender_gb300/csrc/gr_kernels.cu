@@ -1202,6 +1202,65 @@ struct RasterSmem {
   uint32_t next, nlarge, last;
 };
 
+// Final colour and depth of pixel (x, y) of view vw whose visibility key is k:
+// deferred shading of the winning triangle (rasterizer.go:149-176), or Clear
+// and DotGrid when no triangle won; then overlay marks, the crosshair and fog.
+__device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView& vw, int x, int y,
+                                              unsigned long long k, uint32_t& out_c, float& out_z) {
+  const bool face_ids = vw.flags & kViewFaceIds;
+  // overlay marks (k_overlay): the last mark in draw order, if any
+  uint32_t ov = 0;
+  if (vw.flags & 0xC0u) {
+    uint32_t* op = a.ovl_key + vw.pix_base + (size_t)y * (size_t)vw.W + (size_t)x;
+    ov = *op;
+    if (ov) *op = 0u;  // ready for the next frame
+  }
+  // vertexColor (255,161,0,255); edgeColor black, or white without faces (renderer.go:17-19, 192-196)
+  const uint32_t ovc = (ov & 1u) ? 0xFF00A1FFu : ((vw.flags & 0x02u) ? 0xFF000000u : 0xFFFFFFFFu);
+  if (k == BG_KEY) {
+    const bool dot = (x % 10 == 0) && (y % 10 == 0) && x >= 10 && y >= 10;  // DotGrid
+    out_c = ov ? ovc : face_ids ? kNoFace : dot ? 0xFF646464u : 0xFF323232u;
+    out_z = -1.0f;
+  } else {
+    const uint32_t okey = (uint32_t)k & 0x7FFFFFFFu;
+    const uint32_t r = a.rec_of_key[okey];
+    const TriRaster t = a.rast[r];
+    bool inside;
+    float e12f, e20f, al, be, ga;
+    edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
+    const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
+    out_z = z;
+    if (face_ids) {
+      out_c = (okey - 1u) / (uint32_t)kKeysPerFace;  // the face of order key face * 8 + fan + 1
+      return;
+    }
+    const TriShade s = a.shade[r];
+    const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
+    uint32_t c;
+    if (s.tex >= 0) {
+      const float u = fd(fa(fa(fm(al, s.u0w), fm(be, s.u1w)), fm(ga, s.u2w)), z);
+      const float v = fd(fa(fa(fm(al, s.v0w), fm(be, s.v1w)), fm(ga, s.v2w)), z);
+      c = color_intensity(tex_sample(a.texs[s.tex], u, v), I);
+    } else if (s.tex == -2) {
+      const TriColor& tc = a.tcol[r];
+      uint32_t ch[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float cq = fa(fa(fm(al, tc.c[q]), fm(be, tc.c[3 + q])), fm(ga, tc.c[6 + q]));
+        ch[q] = go_u8(fm(fm(cq, 255.0f), I));
+      }
+      c = ch[0] | (ch[1] << 8) | (ch[2] << 16) | 0xFF000000u;
+    } else {
+      c = color_intensity(0xFFC8C8C8u, I);  // faceColor (200,200,200,255)
+    }
+    // a mark of the winner itself or of a later triangle lies on top of the fill
+    out_c = (ov && (ov >> 1) >= okey) ? ovc : c;
+  }
+  if (face_ids) return;
+  if ((vw.flags & 0x100u) && crosshair_hit(vw.W, vw.H, x, y)) out_c = 0xFF00FFFFu;  // (255,255,0,255)
+  if (vw.fog_on) out_c = fog_pixel(out_c, out_z, vw.fog_start, vw.fog_end, vw.fog_color);
+}
+
 // One raster work item: slice `slice` of global tile `tile` of view `view`.
 template <int TS>
 __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, uint32_t slice, int view,
@@ -1331,13 +1390,17 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
         const int incl2 = warp_incl_scan(len);
         const int excl2 = incl2 - len;
         const int total2 = __shfl_sync(FULL_MASK, incl2, 31);
-        for (int h0 = 0; h0 < total2; h0 += 32) {
-          const int h = h0 + (int)lane;
-          const int o2 = owner_lane(excl2, h);
-          const int x = __shfl_sync(FULL_MASK, xl, o2) + h - __shfl_sync(FULL_MASK, excl2, o2);
-          const int yy = __shfl_sync(FULL_MASK, y, o2);
-          const int slot = __shfl_sync(FULL_MASK, own, o2);
-          if (h < total2) depth_covered<TS>(skey, tri[slot], x, yy, tx0, ty0);
+        // two pixels a lane per pass: their depth tests are independent
+        // chains of divisions that overlap
+        for (int h0 = 0; h0 < total2; h0 += 64) {
+          const int ha = h0 + (int)lane, hb = ha + 32;
+          const int oa = owner_lane(excl2, ha), ob = owner_lane(excl2, hb);
+          const int xa = __shfl_sync(FULL_MASK, xl, oa) + ha - __shfl_sync(FULL_MASK, excl2, oa);
+          const int xb = __shfl_sync(FULL_MASK, xl, ob) + hb - __shfl_sync(FULL_MASK, excl2, ob);
+          const int ya = __shfl_sync(FULL_MASK, y, oa), yb = __shfl_sync(FULL_MASK, y, ob);
+          const int sa = __shfl_sync(FULL_MASK, own, oa), sb = __shfl_sync(FULL_MASK, own, ob);
+          if (ha < total2) depth_covered<TS>(skey, tri[sa], xa, ya, tx0, ty0);
+          if (hb < total2) depth_covered<TS>(skey, tri[sb], xb, yb, tx0, ty0);
         }
       }
       __syncwarp();  // lane slots are rewritten by the next chunk
@@ -1401,90 +1464,41 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     __syncthreads();
   }
 
-  // Resolve + deferred shading; Clear and DotGrid for uncovered pixels.
-  constexpr int kPerRow = TS / 4;
-  const int row = tid / kPerRow;
-  const int col = (tid % kPerRow) * 4;
-  const int y = ty0 + row;
-  if (y <= ty1) {
-    uint32_t out_c[4];
-    float out_z[4];
-    const ulonglong2* kp = reinterpret_cast<const ulonglong2*>(skey + row * kStride + col);
-    const ulonglong2 k01 = kp[0], k23 = kp[1];
-    const unsigned long long keys[4] = {k01.x, k01.y, k23.x, k23.y};
+  if (a.pkey) {
+    // the tile's final keys, shaded by k_resolve
+    for (int i = tid; i < TS * TS; i += kThreads) {
+      const int rr = i / TS, cc = i % TS;
+      const int x = tx0 + cc, y = ty0 + rr;
+      if (x <= tx1 && y <= ty1) a.pkey[vw.pix_base + (size_t)y * (size_t)vw.W + (size_t)x] = skey[rr * kStride + cc];
+    }
+  } else {
+    // Resolve + deferred shading, four pixels a thread
+    constexpr int kPerRow = TS / 4;
+    const int row = tid / kPerRow;
+    const int col = (tid % kPerRow) * 4;
+    const int y = ty0 + row;
+    if (y <= ty1) {
+      uint32_t out_c[4];
+      float out_z[4];
+      const ulonglong2* kp = reinterpret_cast<const ulonglong2*>(skey + row * kStride + col);
+      const ulonglong2 k01 = kp[0], k23 = kp[1];
+      const unsigned long long keys[4] = {k01.x, k01.y, k23.x, k23.y};
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int x = tx0 + col + j;
-      const unsigned long long k = keys[j];
-      const bool face_ids = vw.flags & kViewFaceIds;
-      // overlay marks (k_overlay): the last mark in draw order, if any
-      uint32_t ov = 0;
-      if ((vw.flags & 0xC0u) && x <= tx1) {
-        uint32_t* op = a.ovl_key + vw.pix_base + (size_t)y * (size_t)vw.W + (size_t)x;
-        ov = *op;
-        if (ov) *op = 0u;  // ready for the next frame
+      for (int j = 0; j < 4; ++j) {
+        out_c[j] = 0u;
+        out_z[j] = 0.0f;
+        if (tx0 + col + j <= tx1) resolve_pixel(a, vw, tx0 + col + j, y, keys[j], out_c[j], out_z[j]);
       }
-      // vertexColor (255,161,0,255); edgeColor black, or white without faces (renderer.go:17-19, 192-196)
-      const uint32_t ovc = (ov & 1u) ? 0xFF00A1FFu : ((vw.flags & 0x02u) ? 0xFF000000u : 0xFFFFFFFFu);
-      if (k == BG_KEY || x > tx1) {
-        const bool dot = (x % 10 == 0) && (y % 10 == 0) && x >= 10 && y >= 10;  // DotGrid
-        out_c[j] = ov ? ovc : face_ids ? kNoFace : dot ? 0xFF646464u : 0xFF323232u;
-        out_z[j] = -1.0f;
-        continue;
-      }
-      const uint32_t okey = (uint32_t)k & 0x7FFFFFFFu;
-      const uint32_t r = a.rec_of_key[okey];
-      const TriRaster t = a.rast[r];
-      bool inside;
-      float e12f, e20f, al, be, ga;
-      edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
-      const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
-      if (face_ids) {
-        out_c[j] = (okey - 1u) / (uint32_t)kKeysPerFace;  // the face of order key face * 8 + fan + 1
-        out_z[j] = z;
-        continue;
-      }
-      const TriShade s = a.shade[r];
-      const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
-      uint32_t c;
-      if (s.tex >= 0) {
-        const float u = fd(fa(fa(fm(al, s.u0w), fm(be, s.u1w)), fm(ga, s.u2w)), z);
-        const float v = fd(fa(fa(fm(al, s.v0w), fm(be, s.v1w)), fm(ga, s.v2w)), z);
-        c = color_intensity(tex_sample(a.texs[s.tex], u, v), I);
-      } else if (s.tex == -2) {
-        const TriColor& tc = a.tcol[r];
-        uint32_t ch[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const float cq = fa(fa(fm(al, tc.c[q]), fm(be, tc.c[3 + q])), fm(ga, tc.c[6 + q]));
-          ch[q] = go_u8(fm(fm(cq, 255.0f), I));
-        }
-        c = ch[0] | (ch[1] << 8) | (ch[2] << 16) | 0xFF000000u;
+      const int x = tx0 + col;
+      const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
+      if (vw.vec_ok && x + 3 <= tx1) {
+        *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(out_c[0], out_c[1], out_c[2], out_c[3]);
+        *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
       } else {
-        c = color_intensity(0xFFC8C8C8u, I);  // faceColor (200,200,200,255)
-      }
-      // a mark of the winner itself or of a later triangle lies on top of the fill
-      out_c[j] = (ov && (ov >> 1) >= okey) ? ovc : c;
-      out_z[j] = z;
-    }
-    if (vw.flags & (0x100u | kViewFaceIds)) {
-      if (!(vw.flags & kViewFaceIds))
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (crosshair_hit(vw.W, vw.H, tx0 + col + j, y)) out_c[j] = 0xFF00FFFFu;  // (255,255,0,255)
-    }
-    if (vw.fog_on && !(vw.flags & kViewFaceIds))
-#pragma unroll
-      for (int j = 0; j < 4; ++j) out_c[j] = fog_pixel(out_c[j], out_z[j], vw.fog_start, vw.fog_end, vw.fog_color);
-    const int x = tx0 + col;
-    const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
-    if (vw.vec_ok && x + 3 <= tx1) {
-      *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(out_c[0], out_c[1], out_c[2], out_c[3]);
-      *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
-    } else {
-      for (int j = 0; j < 4 && x + j <= tx1; ++j) {
-        vw.out_rgba[o + j] = out_c[j];
-        vw.out_z[o + j] = out_z[j];
+        for (int j = 0; j < 4 && x + j <= tx1; ++j) {
+          vw.out_rgba[o + j] = out_c[j];
+          vw.out_z[o + j] = out_z[j];
+        }
       }
     }
   }
@@ -1683,6 +1697,32 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_resolve: one thread per pixel of every view; shades the winners whose
+// keys k_raster stored (the shading of resolve_pixel, at full occupancy so
+// that its chain of dependent loads overlaps across many warps).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
+  const unsigned long long p = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
+  if (p >= a.total_pixels) return;
+  int v = 0;
+  if (a.num_views > 1) {  // last view whose first pixel <= p
+    int hi = a.num_views - 1;
+    while (v < hi) {
+      const int mid = (v + hi + 1) >> 1;
+      if (a.views[mid].pix_base <= p) v = mid; else hi = mid - 1;
+    }
+  }
+  const DevView& vw = a.views[v];
+  const uint32_t o = (uint32_t)(p - vw.pix_base);
+  const int y = (int)(o / (uint32_t)vw.W), x = (int)(o - (uint32_t)y * (uint32_t)vw.W);
+  uint32_t c;
+  float z;
+  resolve_pixel(a, vw, x, y, a.pkey[p], c, z);
+  vw.out_rgba[o] = c;
+  vw.out_z[o] = z;
+}
+
 int raster_grid(int tile_shift, int waves) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
@@ -1730,6 +1770,10 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
   else
     k_raster<32><<<a.raster_ctas, RasterShape<32>::kThreads, 0, s>>>(a);
   ++n;
+  if (a.pkey && a.total_pixels) {
+    k_resolve<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
+    ++n;
+  }
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
   if (launches) *launches = n;
   return (int)cudaGetLastError();

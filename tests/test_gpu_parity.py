@@ -192,3 +192,39 @@ def test_alternating_scenes_replay_captured_frames(ctx):
         for (rgba0, z0, tpf0), up in zip(first, ups):
             rgba, z, tpf = up.render()
             assert tpf == tpf0 and np.array_equal(rgba, rgba0) and np.array_equal(z.view(np.uint32), z0.view(np.uint32))
+
+
+def test_page_locked_host_outputs(ctx):
+    """Outputs in page-locked host memory are written by the kernels through
+    their device addresses (no copy after the frame); pageable outputs are
+    copied.  Both give the oracle's frame, and both count as device-to-host
+    bytes."""
+    import ctypes as C
+
+    from gorender_gb300 import _native as N
+
+    L = N.lib()
+    sc = scenes.scene_heightfield_1280x720(n=129)
+    up = gr.UploadedScene(ctx, sc)
+    npx = sc.width * sc.height
+    hp = C.c_void_p()
+    N.check(L.gr_host_alloc(npx * 8, C.byref(hp)))
+    try:
+        buf = (C.c_uint8 * (npx * 8)).from_address(hp.value)
+        arr = np.frombuffer(buf, np.uint8)
+        arr[:] = 0xAB
+        tpf = C.c_int64()
+        N.check(L.gr_draw(ctx.handle, up.items, len(sc.objects), C.byref(up.params), hp.value, hp.value + npx * 4,
+                          C.byref(tpf)))
+        rgba = arr[:npx * 4].reshape(sc.height, sc.width, 4).copy()
+        z = arr[npx * 4:].view(np.float32).reshape(sc.height, sc.width).copy()
+        h2d, d2h = C.c_int64(), C.c_int64()
+        N.check(L.gr_context_last_transfer_bytes(ctx.handle, C.byref(h2d), C.byref(d2h)))
+    finally:
+        N.check(L.gr_host_free(hp))
+    ref_rgba, ref_z, ref_tpf, st = oracle.draw_scene(sc, items_override=up.matrices, nthreads=4)
+    assert st == 0 and tpf.value == ref_tpf
+    assert np.array_equal(rgba, ref_rgba) and np.array_equal(z.view(np.uint32), ref_z.view(np.uint32))
+    assert d2h.value >= npx * 8
+    rgba2, z2, tpf2 = up.render()  # pageable numpy outputs: the copy path
+    assert tpf2 == ref_tpf and np.array_equal(rgba2, ref_rgba)
