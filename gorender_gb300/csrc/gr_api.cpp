@@ -464,6 +464,13 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   uint64_t vert_total = 0;
   int vert_blocks = 0;
   int live = 0;
+  uint64_t all_faces = 0;
+  for (int i = 0; i < n; ++i) {
+    const int m = items[i].mesh;
+    if (m >= 0 && m < (int)c->meshes.size() && c->meshes[m].alive) all_faces += (uint64_t)c->meshes[m].nf;
+  }
+  const int project_g = project_faces_per_lane(all_faces);
+  const int project_faces = kProjectThreads * project_g;
   for (int i = 0; i < n; ++i) {
     const int m = items[i].mesh;
     if (m < 0 || m >= (int)c->meshes.size() || !c->meshes[m].alive)
@@ -492,7 +499,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     d.vert_block_base = vert_blocks;
     vert_total += (uint64_t)mr.nv;
     vert_blocks += (mr.nv + 255) / 256;
-    blocks += (mr.nf + kProjectThreads - 1) / kProjectThreads;
+    blocks += (mr.nf + project_faces - 1) / project_faces;
     // every item gets a k_light block range (empty for non-Gouraud items) so the
     // kernel's block -> item search sees non-decreasing bases
     d.light_base = (int)light_total;
@@ -551,6 +558,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.tile_shift = c->tile_shift;
   a.num_items = live;
   a.total_blocks = blocks;
+  a.project_g = project_g;
   a.bin_cap = c->bin_cap;
   a.rec_cap = c->rec_cap;
   a.big_cap = c->big_cap;

@@ -15,6 +15,11 @@ constexpr int kNarrowLimit = 16384;           // |screen coordinate| < 2^14 => i
 constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes fans into <= 7
 constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
 constexpr int kProjectThreads = 256;
+// k_project: faces a thread tests before the survivors are compacted (1, 2
+// or 4, by the frame's face count: enough blocks to fill the GPU first)
+__host__ __device__ constexpr int project_faces_per_lane(unsigned long long faces) {
+  return faces >= 2000000ull ? 4 : faces >= 1000000ull ? 2 : 1;
+}
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
 constexpr int kStageSlots = 3;                // pinned staging slots for back-to-back async draws
 constexpr int kRasterMaxSlices = 32;          // CTAs that may share one tile's bin
@@ -152,6 +157,7 @@ struct FrameArgs {
   int tile_shift;                   // raster tile = (1 << tile_shift)^2 pixels (4 or 5)
   int num_items;
   int total_blocks;
+  int project_g;                    // k_project faces a thread (project_faces_per_lane)
   uint32_t bin_cap;
   uint32_t rec_cap;
   uint32_t big_cap;

@@ -1,19 +1,29 @@
 // gr_kernels.cu -- sm_103a kernels of the frame pipeline.
 //
-// A frame runs as three kernels on one stream:
-//   k_project  one thread per face: vertex transform, backface cull, lighting,
-//              frustum clip, perspective divide + screen map, one-tile bin test
-//              and edge-function setup; triangles are compacted with a warp
-//              scan + one atomic per warp and appended to per-tile bins with
-//              warp-aggregated atomics (__match_any_sync) or, when they span
-//              more than four tiles, to a multi-tile queue.
-//   k_bin_big  one CTA per multi-tile triangle: appends it to every 32x32 tile
-//              its edge functions can reach.
-//   k_raster   one CTA per 32x32 tile: resolves visibility in shared memory as
-//              a 64-bit max of (ordered zRec, draw-order key), walking 8x8
-//              pixel blocks per warp; then shades each pixel once for its
-//              winner (deferred), fused with Clear + DotGrid, and writes the
-//              tile back with 16-byte stores.
+// A frame runs as a short sequence of kernels on one stream (captured once
+// into a CUDA graph and replayed):
+//   k_light    Gouraud intensity once per vertex normal.
+//   k_vertex   clip-space position and unsnapped screen x, y once per vertex.
+//   k_project  faces in groups of 32 x G per warp: backface and frustum tests
+//              on every face, survivors compacted, then for full warps of
+//              survivors the attributes, screen vertices, bin test (TPF) and
+//              edge-function setup; records are appended with one atomic per
+//              warp and binned with warp-aggregated atomics (__match_any_sync)
+//              or, past four tiles, queued for k_bin_big.  Straddling faces
+//              go to k_clip (the general clipper, one warp per face).
+//   k_bin_big  one warp per multi-tile triangle: appends it to every tile its
+//              edge functions can reach.
+//   k_plan     splits heavy tiles into slices by estimated cost and orders
+//              the work queue heaviest first.
+//   k_raster   persistent CTAs over the queue, one TS x TS tile slice each:
+//              visibility in shared memory as a 64-bit max of (ordered zRec,
+//              draw-order key); each row of a footprint is narrowed to its
+//              exact covered span, so only covered pixels reach the depth
+//              test; slices merge through global keys.  Many views: the
+//              tile is shaded in place.  One view: the final keys are stored
+//              and
+//   k_resolve  shades every pixel once for its winner (deferred), with Clear,
+//              DotGrid, overlays, crosshair and fog, one thread per pixel.
 //
 // Bit-exactness: every float operation is an explicit round-to-nearest
 // intrinsic in the reference's source order (no contraction; the files are
@@ -534,10 +544,12 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_project: one thread per face; everything but the general clipper.
+// k_project: G faces a thread in the cheap pass, full warps of survivors in
+// the heavy one; everything but the general clipper.
 // ---------------------------------------------------------------------------
 // 4 CTAs per SM (64 registers a thread): the face pass is latency-bound, so
 // resident warps matter more than the few registers spilled.
+template <int G>
 __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
@@ -583,132 +595,160 @@ __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs 
 
   const uint32_t fl = vw.flags;
   const int W = vw.W, H = vw.H;
-  const int f = ((int)blockIdx.x - it.block_base) * kProjectThreads + tid;
-  const bool valid = f < it.nf;
   const unsigned lane = lane_id();
+  const int warp = tid >> 5;
 
-  bool emit = false;   // this face yields one record
-  bool general = false;  // this face needs the general clipper (k_clip)
-  int ntpf = 0;
-  int tex = -1;
-  SV s0, s1, s2;
-  if (valid) {
-    const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
-    // clip-space corners from k_vertex (the same arithmetic, done once per vertex)
-    const float4 c0 = __ldg(a.vclip + it.vert_base + i0), c1 = __ldg(a.vclip + it.vert_base + i1),
-                 c2 = __ldg(a.vclip + it.vert_base + i2);
-    const V4 v0{c0.x, c0.y, c0.z, c0.w}, v1{c1.x, c1.y, c1.z, c1.w}, v2{c2.x, c2.y, c2.z, c2.w};
-    bool draw = !(fl & 0x04u) || facing_camera(v0, v1, v2);  // BackfaceCulling
-    // Frustum clipping (renderer.go:349-359).  At the first plane, in clipping
-    // order, where not all three vertices are inside: all outside means the
-    // polygon reaching that plane is still the face itself (every earlier pass
-    // only rotated it), so ClipTriangle returns no triangle; a mix needs the
-    // general clipper.  With no such plane the six passes rotate the face back
-    // to itself and it passes through unchanged.
-    if (draw && (fl & 0x01u) && vis != 2) {
-      for (int i = 0; i < 6; ++i) {
-        const int m = (int)plane_inside(i, v0) + (int)plane_inside(i, v1) + (int)plane_inside(i, v2);
-        if (m == 3) continue;
-        if (m == 0) draw = false;
-        else general = true;
-        break;
+  // Pass 1, every face of the warp's group: backface and frustum tests (the
+  // clip-space corners come from k_vertex: the same arithmetic, done once per
+  // vertex).  Faces for the general clipper are queued for k_clip; faces that
+  // survive whole are compacted into the warp's list, so that pass 2 runs on
+  // full warps (most faces of a closed mesh face away or miss the screen).
+  __shared__ int s_surv[kProjectThreads / 32][32 * G];
+  int* surv = s_surv[warp];
+  int nsurv = 0;
+  const int fgroup = ((int)blockIdx.x - it.block_base) * (kProjectThreads * G) + warp * (32 * G);
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    const int f = fgroup + k * 32 + (int)lane;
+    bool draw = false;
+    bool general = false;  // this face needs the general clipper (k_clip)
+    if (f < it.nf) {
+      const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
+      const float4 c0 = __ldg(a.vclip + it.vert_base + i0), c1 = __ldg(a.vclip + it.vert_base + i1),
+                   c2 = __ldg(a.vclip + it.vert_base + i2);
+      const V4 v0{c0.x, c0.y, c0.z, c0.w}, v1{c1.x, c1.y, c1.z, c1.w}, v2{c2.x, c2.y, c2.z, c2.w};
+      draw = !(fl & 0x04u) || facing_camera(v0, v1, v2);  // BackfaceCulling
+      // Frustum clipping (renderer.go:349-359).  At the first plane, in
+      // clipping order, where not all three vertices are inside: all outside
+      // means the polygon reaching that plane is still the face itself (every
+      // earlier pass only rotated it), so ClipTriangle returns no triangle; a
+      // mix needs the general clipper.  With no such plane the six passes
+      // rotate the face back to itself and it passes through unchanged.
+      if (draw && (fl & 0x01u) && vis != 2) {
+        for (int i = 0; i < 6; ++i) {
+          const int m = (int)plane_inside(i, v0) + (int)plane_inside(i, v1) + (int)plane_inside(i, v2);
+          if (m == 3) continue;
+          if (m == 0) draw = false;
+          else general = true;
+          break;
+        }
       }
     }
-    if (draw && !general) {
-      PV p0, p1, p2;
-      face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
-      s0 = sv_of(__ldg(a.vscr + it.vert_base + i0), v0.w, p0);
-      s1 = sv_of(__ldg(a.vscr + it.vert_base + i1), v1.w, p1);
-      s2 = sv_of(__ldg(a.vscr + it.vert_base + i2), v2.w, p2);
-      if (bin_test(s0, s1, s2, (float)W, (float)H)) {
-        ntpf = 1;
-        Setup s;
-        // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
-        emit = (fl & 0x02u) && setup_tri(s0, s1, s2, W, H, s);
+    // Faces for the general clipper: one atomic per warp.
+    const unsigned gm = __ballot_sync(FULL_MASK, general);
+    if (gm) {
+      uint32_t qb = 0;
+      const int ldr = __ffs(gm) - 1;
+      if ((int)lane == ldr) qb = atomicAdd(&a.work->nclip, (uint32_t)__popc(gm));
+      qb = __shfl_sync(FULL_MASK, qb, ldr);
+      if (general) {
+        const uint32_t q = qb + __popc(gm & ((1u << lane) - 1u));
+        if (q < a.clip_cap) a.clip[q] = make_uint2((uint32_t)item, (uint32_t)f);
+        else atomicMax(&a.work->clip_need, q + 1);
       }
     }
+    const bool keep = draw && !general;
+    const unsigned km = __ballot_sync(FULL_MASK, keep);
+    if (keep) surv[nsurv + __popc(km & ((1u << lane) - 1u))] = f;
+    nsurv += __popc(km);
   }
+  __syncwarp();
 
-  // Faces for the general clipper: one atomic per warp.
-  const unsigned gm = __ballot_sync(FULL_MASK, general);
-  if (gm) {
-    uint32_t qb = 0;
-    const int ldr = __ffs(gm) - 1;
-    if ((int)lane == ldr) qb = atomicAdd(&a.work->nclip, (uint32_t)__popc(gm));
-    qb = __shfl_sync(FULL_MASK, qb, ldr);
-    if (general) {
-      const uint32_t q = qb + __popc(gm & ((1u << lane) - 1u));
-      if (q < a.clip_cap) a.clip[q] = make_uint2((uint32_t)item, (uint32_t)f);
-      else atomicMax(&a.work->clip_need, q + 1);
-    }
-  }
-
-  // TPF: one atomic per warp (all faces of a block belong to one view).
-  const int wt = __reduce_add_sync(FULL_MASK, ntpf);
-  if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
-  if (fl & 0xC0u)  // ShowEdges / ShowVertices: every binned triangle leaves marks
-    emit_overlay(a, ntpf != 0, s0, s1, s2, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u, it.view);
-
-  // Compact records: one atomic per warp, lane offsets from the ballot.
-  const unsigned em = __ballot_sync(FULL_MASK, emit);
-  if (em == 0) return;
-  uint32_t base = 0;
-  const int ldr = __ffs(em) - 1;
-  if ((int)lane == ldr) {
-    base = atomicAdd(&a.work->nrec, (uint32_t)__popc(em));
-    if (base + (uint32_t)__popc(em) > a.rec_cap) atomicMax(&a.work->rec_need, base + (uint32_t)__popc(em));
-  }
-  base = __shfl_sync(FULL_MASK, base, ldr);
-  const uint32_t r = base + __popc(em & ((1u << lane) - 1u));
-  const bool ok = emit && r < a.rec_cap;
-  uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
-  int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
-  if (ok) {
-    Setup s;
-    setup_tri(s0, s1, s2, W, H, s);
-    write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
-    pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
-    tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
-    tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
-    ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
-    ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
-  }
-  const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
-  // single-tile triangles: warp-aggregated append per distinct tile
-  const bool one = ntiles == 1;
-  const unsigned m1 = __ballot_sync(FULL_MASK, one);
-  if (one) {
-    const uint32_t tile = vw.tile_base + ty0 * (uint32_t)vw.tiles_x + tx0;
-    const unsigned grp = __match_any_sync(m1, tile);
-    const int leader = __ffs(grp) - 1;
-    const unsigned rank = __popc(grp & ((1u << lane) - 1u));
-    uint32_t pos = 0;
-    const uint32_t box = (uint32_t)((pbx1 - pbx0 + 1) * (pby1 - pby0 + 1));
-    if (box > (uint32_t)kSmallBox) atomicAdd(&a.tile_cost[tile], box);
-    if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
-    pos = __shfl_sync(grp, pos, leader) + rank;
-    bin_store(a, tile, pos, r);
-  }
-  // two to four tiles: direct appends
-  if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
-    for (uint32_t ty = ty0; ty <= ty1; ++ty)
-      for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-        bin_store(a, tile, bin_append(a, tile, tile_box(pbx0, pbx1, pby0, pby1, tx, ty, a.tile_shift)), r);
+  // Pass 2, the surviving faces 32 at a time: attributes, screen vertices,
+  // the bin test (TPF), setup, the record and its bins.
+  for (int k0 = 0; k0 < nsurv; k0 += 32) {
+    const bool valid = k0 + (int)lane < nsurv;
+    const int f = valid ? surv[k0 + lane] : 0;
+    bool emit = false;   // this face yields one record
+    int ntpf = 0;
+    int tex = -1;
+    SV s0, s1, s2;
+    if (valid) {
+      const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
+      const float w0 = __ldg(&a.vclip[it.vert_base + i0].w), w1 = __ldg(&a.vclip[it.vert_base + i1].w),
+                  w2 = __ldg(&a.vclip[it.vert_base + i2].w);
+      {
+        PV p0, p1, p2;
+        face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
+        s0 = sv_of(__ldg(a.vscr + it.vert_base + i0), w0, p0);
+        s1 = sv_of(__ldg(a.vscr + it.vert_base + i1), w1, p1);
+        s2 = sv_of(__ldg(a.vscr + it.vert_base + i2), w2, p2);
+        if (bin_test(s0, s1, s2, (float)W, (float)H)) {
+          ntpf = 1;
+          Setup s;
+          // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
+          emit = (fl & 0x02u) && setup_tri(s0, s1, s2, W, H, s);
+        }
       }
-  }
-  // more: the multi-tile queue, one atomic per warp
-  const bool many = ntiles > (uint32_t)kBinDirectMax;
-  const unsigned mm = __ballot_sync(FULL_MASK, many);
-  if (mm) {
-    uint32_t qb = 0;
-    const int l2 = __ffs(mm) - 1;
-    if ((int)lane == l2) qb = atomicAdd(&a.work->nbig, (uint32_t)__popc(mm));
-    qb = __shfl_sync(FULL_MASK, qb, l2);
-    if (many) {
-      const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
-      if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)it.view);
-      else atomicMax(&a.work->big_need, q + 1);
+    }
+
+    // TPF: one atomic per warp (all faces of a block belong to one view).
+    const int wt = __reduce_add_sync(FULL_MASK, ntpf);
+    if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
+    if (fl & 0xC0u)  // ShowEdges / ShowVertices: every binned triangle leaves marks
+      emit_overlay(a, ntpf != 0, s0, s1, s2, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u, it.view);
+
+    // Compact records: one atomic per warp, lane offsets from the ballot.
+    const unsigned em = __ballot_sync(FULL_MASK, emit);
+    if (em == 0) continue;
+    uint32_t base = 0;
+    const int ldr = __ffs(em) - 1;
+    if ((int)lane == ldr) {
+      base = atomicAdd(&a.work->nrec, (uint32_t)__popc(em));
+      if (base + (uint32_t)__popc(em) > a.rec_cap) atomicMax(&a.work->rec_need, base + (uint32_t)__popc(em));
+    }
+    base = __shfl_sync(FULL_MASK, base, ldr);
+    const uint32_t r = base + __popc(em & ((1u << lane) - 1u));
+    const bool ok = emit && r < a.rec_cap;
+    uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
+    int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
+    if (ok) {
+      Setup s;
+      setup_tri(s0, s1, s2, W, H, s);
+      write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
+      pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
+      tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
+      tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
+      ty0 = (uint32_t)s.r.by0 >> a.tile_shift;
+      ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
+    }
+    const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
+    // single-tile triangles: warp-aggregated append per distinct tile
+    const bool one = ntiles == 1;
+    const unsigned m1 = __ballot_sync(FULL_MASK, one);
+    if (one) {
+      const uint32_t tile = vw.tile_base + ty0 * (uint32_t)vw.tiles_x + tx0;
+      const unsigned grp = __match_any_sync(m1, tile);
+      const int leader = __ffs(grp) - 1;
+      const unsigned rank = __popc(grp & ((1u << lane) - 1u));
+      uint32_t pos = 0;
+      const uint32_t box = (uint32_t)((pbx1 - pbx0 + 1) * (pby1 - pby0 + 1));
+      if (box > (uint32_t)kSmallBox) atomicAdd(&a.tile_cost[tile], box);
+      if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
+      pos = __shfl_sync(grp, pos, leader) + rank;
+      bin_store(a, tile, pos, r);
+    }
+    // two to four tiles: direct appends
+    if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
+      for (uint32_t ty = ty0; ty <= ty1; ++ty)
+        for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+          const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
+          bin_store(a, tile, bin_append(a, tile, tile_box(pbx0, pbx1, pby0, pby1, tx, ty, a.tile_shift)), r);
+        }
+    }
+    // more: the multi-tile queue, one atomic per warp
+    const bool many = ntiles > (uint32_t)kBinDirectMax;
+    const unsigned mm = __ballot_sync(FULL_MASK, many);
+    if (mm) {
+      uint32_t qb = 0;
+      const int l2 = __ffs(mm) - 1;
+      if ((int)lane == l2) qb = atomicAdd(&a.work->nbig, (uint32_t)__popc(mm));
+      qb = __shfl_sync(FULL_MASK, qb, l2);
+      if (many) {
+        const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
+        if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)it.view);
+        else atomicMax(&a.work->big_need, q + 1);
+      }
     }
   }
 }
@@ -1745,7 +1785,9 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     }
     k_vertex<<<a.vert_blocks, 256, 0, s>>>(a);
     ++n;
-    k_project<<<a.total_blocks, kProjectThreads, 0, s>>>(a);
+    if (a.project_g == 4) k_project<4><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
+    else if (a.project_g == 2) k_project<2><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
+    else k_project<1><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
     if (a.flags_any & 0x01u) {

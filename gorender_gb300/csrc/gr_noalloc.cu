@@ -180,7 +180,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     d.face_base = fb;
     d.block_base = blocks;
     d.view = 0;
-    blocks += (m.num_faces + kProjectThreads - 1) / kProjectThreads;
+    blocks += (m.num_faces + kProjectThreads - 1) / kProjectThreads;  // one face a thread (kMaxFaces is small)
     d.vert_base = vert_total;
     d.vert_block_base = vert_blocks;
     vert_total += (uint32_t)m.num_vertices;
@@ -238,6 +238,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.tile_shift = 5;
   a.num_items = live;
   a.total_blocks = blocks;
+  a.project_g = 1;
   a.bin_cap = kBinCap;
   a.rec_cap = kRecCap;
   a.big_cap = kQueueCap;
