@@ -498,7 +498,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     d.vert_base = (uint32_t)vert_total;
     d.vert_block_base = vert_blocks;
     vert_total += (uint64_t)mr.nv;
-    vert_blocks += (mr.nv + 255) / 256;
+    vert_blocks += (mr.nv + 256 * project_g - 1) / (256 * project_g);
     blocks += (mr.nf + project_faces - 1) / project_faces;
     // every item gets a k_light block range (empty for non-Gouraud items) so the
     // kernel's block -> item search sees non-decreasing bases
@@ -506,7 +506,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     d.light_block_base = light_blocks;
     if (gouraud && mr.nn > 0) {
       light_total += (uint64_t)mr.nn;
-      light_blocks += (mr.nn + 255) / 256;
+      light_blocks += (mr.nn + 256 * project_g - 1) / (256 * project_g);
     }
   }
   if (faces >= (1ull << 28)) return fail(GR_ERR_UNSUPPORTED, "more than 2^28 faces in one frame");

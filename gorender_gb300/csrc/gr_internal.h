@@ -157,7 +157,8 @@ struct FrameArgs {
   int tile_shift;                   // raster tile = (1 << tile_shift)^2 pixels (4 or 5)
   int num_items;
   int total_blocks;
-  int project_g;                    // k_project faces a thread (project_faces_per_lane)
+  int project_g;                    // k_project faces a thread (project_faces_per_lane); k_light and
+                                    // k_vertex take as many normals / vertices a thread
   uint32_t bin_cap;
   uint32_t rec_cap;
   uint32_t big_cap;

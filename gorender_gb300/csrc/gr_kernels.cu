@@ -414,14 +414,18 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
     in0 = in1 = in2 = 0.5f;
   }
   p0.in = in0; p1.in = in1; p2.in = in2;
-  if (it.uv) {
+  const int t = it.tex ? __ldg(it.tex + f) : -1;
+  tex = ((fl & 0x20u) && t >= 0) ? t : (it.vcol ? -2 : -1);  // renderer.go:176-178
+  // texture coordinates reach the shading only through a texture, vertex
+  // colours only without one: the other is left at zero
+  if (tex >= 0 && it.uv) {
     const float2* uv = reinterpret_cast<const float2*>(it.uv + 6 * (size_t)f);
     const float2 t0 = __ldg(uv), t1 = __ldg(uv + 1), t2 = __ldg(uv + 2);
     p0.u = t0.x; p0.v = t0.y; p1.u = t1.x; p1.v = t1.y; p2.u = t2.x; p2.v = t2.y;
   } else {
     p0.u = p0.v = p1.u = p1.v = p2.u = p2.v = 0.0f;
   }
-  if (it.vcol) {
+  if (tex == -2) {
     const float* c0 = it.vcol + 3 * (size_t)i0;
     const float* c1 = it.vcol + 3 * (size_t)i1;
     const float* c2 = it.vcol + 3 * (size_t)i2;
@@ -431,8 +435,6 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
   } else {
     p0.r = p0.g = p0.b = p1.r = p1.g = p1.b = p2.r = p2.g = p2.b = 0.0f;
   }
-  const int t = it.tex ? __ldg(it.tex + f) : -1;
-  tex = ((fl & 0x20u) && t >= 0) ? t : (it.vcol ? -2 : -1);  // renderer.go:176-178
 }
 
 // Writes record r of a set-up triangle (raster part, int64 edges, shading).
@@ -449,9 +451,13 @@ __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Set
     for (int q = 0; q < 5; ++q) wd[q] = ws[q];
   }
   TriShade sh;
-  sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);  // rasterizer.go:132-137
-  sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
-  sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
+  if (tex >= 0) {  // read by the shading only through a texture
+    sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);  // rasterizer.go:132-137
+    sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
+    sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
+  } else {
+    sh.u0w = sh.v0w = sh.u1w = sh.v1w = sh.u2w = sh.v2w = 0.0f;
+  }
   sh.i0 = q0.in; sh.i1 = q1.in; sh.i2 = q2.in;
   sh.tex = tex;
   sh.pad[0] = sh.pad[1] = 0.0f;
@@ -507,6 +513,7 @@ __device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
 // does not depend on the face that uses it, so the face pass gathers these
 // instead of transforming each corner again.
 // ---------------------------------------------------------------------------
+template <int G>
 __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_S[8];
@@ -517,11 +524,16 @@ __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
   if (threadIdx.x < 16) s_mvp[threadIdx.x] = it.mvp[threadIdx.x];
   if (threadIdx.x < 8) s_S[threadIdx.x] = a.views[it.view].S[threadIdx.x];
   __syncthreads();
-  const int v = ((int)blockIdx.x - it.vert_block_base) * 256 + (int)threadIdx.x;
-  if (v >= it.nv) return;
-  const V4 c = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)v));
-  a.vclip[it.vert_base + v] = make_float4(c.x, c.y, c.z, c.w);
-  a.vscr[it.vert_base + v] = screen_of(c, s_S);
+  const int v0 = ((int)blockIdx.x - it.vert_block_base) * (256 * G) + (int)threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    const int v = v0 + k * 256;
+    if (v < it.nv) {
+      const V4 c = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)v));
+      a.vclip[it.vert_base + v] = make_float4(c.x, c.y, c.z, c.w);
+      a.vscr[it.vert_base + v] = screen_of(c, s_S);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -530,6 +542,7 @@ __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
 // face corner (renderer.go:327-333); the value depends only on the normal
 // index, so computing it once per normal gives the same bits.
 // ---------------------------------------------------------------------------
+template <int G>
 __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
   __shared__ float s_world[16];
   __shared__ int s_item;
@@ -539,8 +552,12 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
   if (threadIdx.x < 16) s_world[threadIdx.x] = it.world[threadIdx.x];
   __syncthreads();
   if (!gouraud(a, it)) return;
-  const int n = ((int)blockIdx.x - it.light_block_base) * 256 + (int)threadIdx.x;
-  if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.views[it.view].L);
+  const int n0 = ((int)blockIdx.x - it.light_block_base) * (256 * G) + (int)threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    const int n = n0 + k * 256;
+    if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.views[it.view].L);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1780,10 +1797,14 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
   if (events) cudaEventRecord((cudaEvent_t)events[0], s);
   if (a.total_blocks > 0) {
     if (a.light_blocks > 0) {
-      k_light<<<a.light_blocks, 256, 0, s>>>(a);
+      if (a.project_g == 4) k_light<4><<<a.light_blocks, 256, 0, s>>>(a);
+      else if (a.project_g == 2) k_light<2><<<a.light_blocks, 256, 0, s>>>(a);
+      else k_light<1><<<a.light_blocks, 256, 0, s>>>(a);
       ++n;
     }
-    k_vertex<<<a.vert_blocks, 256, 0, s>>>(a);
+    if (a.project_g == 4) k_vertex<4><<<a.vert_blocks, 256, 0, s>>>(a);
+    else if (a.project_g == 2) k_vertex<2><<<a.vert_blocks, 256, 0, s>>>(a);
+    else k_vertex<1><<<a.vert_blocks, 256, 0, s>>>(a);
     ++n;
     if (a.project_g == 4) k_project<4><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     else if (a.project_g == 2) k_project<2><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
