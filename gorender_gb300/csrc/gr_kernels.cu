@@ -831,8 +831,21 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
     }
     int count = 3;
     bool overflow = false;
+    // A pass whose plane has every vertex inside emits A for every edge b
+    // (a = (b+1) % count): the polygon rotated by one.  Such passes only
+    // advance `rot` (logical vertex i sits on lane (i + rot) % count); the
+    // rotation is applied before the next pass that cuts, and at the end.
+    int rot = 0;
     for (int pi = 0; pi < 6 && count > 0; ++pi) {
       const bool act = lane < count;
+      if (__all_sync(FULL_MASK, !act || plane_inside(pi, v.p))) {
+        rot = rot + 1 == count ? 0 : rot + 1;
+        continue;
+      }
+      if (rot) {
+        v = shfl_pv(v, (lane + rot) % count);
+        rot = 0;
+      }
       const PV A = shfl_pv(v, (lane + 1 < count) ? lane + 1 : 0);  // a = (b+1) % count
       const bool inA = act && plane_inside(pi, A.p);
       const bool inB = act && plane_inside(pi, v.p);
@@ -875,6 +888,7 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
       continue;
     }
     if (count < 3) continue;  // Polygon.Triangulate returns nothing
+    if (rot) v = shfl_pv(v, (lane + rot) % count);
     const DevView& vw = a.views[it.view];
     const SV sv = to_screen(v, vw.S);  // lane k: polygon vertex k
     const SV s0 = shfl_sv(sv, 0), s1 = shfl_sv(sv, lane + 1 < 9 ? lane + 1 : 0),
