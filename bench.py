@@ -197,9 +197,10 @@ def run_ours(args):
         kms += np.array(buf[:])
         ctx.flush_l2()
     kms /= kprof
-    # the profiled pass brackets three phases: k_light + k_project | k_clip +
-    # k_bin_big | k_plan + k_raster (k_plan is a one-thread-per-tile scan)
-    names = ["k_project", "k_bin_big", "k_raster"]
+    # the profiled pass brackets three stages: k_light + k_vertex + k_project |
+    # k_clip + k_bin_big | k_plan + k_raster + k_resolve (k_plan is a
+    # one-thread-per-tile scan; k_resolve shades the one view's pixels)
+    names = ["project_stage", "bin_stage", "raster_stage"]
     top = int(np.argmax(kms))
     ab = algorithmic_bytes(scene)
     top_bytes = {0: ab["project"], 1: 0, 2: ab["raster"]}[top]
@@ -260,6 +261,9 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(top_bytes),
                      "kernel_ms": {nm: round(float(v), 5) for nm, v in zip(names, kms)},
+                     "stages": {"project_stage": "k_light + k_vertex + k_project",
+                                "bin_stage": "k_clip + k_bin_big",
+                                "raster_stage": "k_plan + k_raster + k_resolve"},
                      "frame_algorithmic_bytes": int(ab["frame"])},
         "gpu_launches": int(launches_per_frame * args.steps),
         "clocks": sampler.summary(),
