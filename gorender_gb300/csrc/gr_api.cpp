@@ -75,6 +75,9 @@ struct FrameGraph {
 struct gr_context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux_stream = nullptr;  // second branch of a frame (AuxStream)
+  cudaEvent_t aux_ev[4] = {};
+  AuxStream aux{};
   std::mutex mu;
   std::vector<MeshRec> meshes;
   std::vector<TexRec> texs;
@@ -628,7 +631,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
     cudaGraph_t g = nullptr;
     int n = 0;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      const int err = launch_frame(a, big_blocks, c->stream, &n, nullptr);
+      const int err = launch_frame(a, big_blocks, c->stream, &n, nullptr, &c->aux);
       const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (!err && e == cudaSuccess && g && cudaGraphInstantiate(&fg.exec, g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
@@ -644,7 +647,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
       cudaGetLastError();  // capture failed: fall back to plain launches
     }
   }
-  int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events);
+  int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events, &c->aux);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
   return GR_OK;
 }
@@ -780,6 +783,13 @@ int32_t gr_context_create(int32_t device, gr_context** out) {
   for (int i = 0; i < 64 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->events[i]);
   for (int i = 0; i < kStageSlots && e == cudaSuccess; ++i)
     e = cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&c->aux_ev[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) {
+    c->aux.stream = c->aux_stream;
+    c->aux.fork[0] = c->aux_ev[0]; c->aux.join[0] = c->aux_ev[1];
+    c->aux.fork[1] = c->aux_ev[2]; c->aux.join[1] = c->aux_ev[3];
+  }
   if (e != cudaSuccess) {
     gr_context_destroy(c);
     return fail(GR_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
@@ -815,6 +825,8 @@ int32_t gr_context_destroy(gr_context* c) {
   for (auto& ev : c->stage_ev) if (ev) cudaEventDestroy(ev);
   for (auto& fg : c->frame_graphs)
     if (fg.exec) cudaGraphExecDestroy(fg.exec);
+  for (auto& ev : c->aux_ev) if (ev) cudaEventDestroy(ev);
+  if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GR_OK;
@@ -1078,7 +1090,7 @@ int32_t batch_capture(gr_batch* b) {
   if (st) return st;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  int err = launch_frame(pr.a, kBigBlocks, c->stream, &b->launches, nullptr);
+  int err = launch_frame(pr.a, kBigBlocks, c->stream, &b->launches, nullptr, &c->aux);
   cudaError_t e2 = cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream);
   cudaError_t e3 = cudaMemcpyAsync(c->h_view_tpf, c->view_tpf_out, sizeof(unsigned long long) * nv,
                                    cudaMemcpyDeviceToHost, c->stream);

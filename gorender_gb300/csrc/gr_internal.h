@@ -260,7 +260,15 @@ int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start
 // Kernel launchers (gr_kernels.cu).
 // events (optional): 4 cudaEvent_t recorded before k_project, after k_project,
 // after k_bin_big and after k_raster.
-int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events);
+// A second stream and its fork / join events (created with timing off) for
+// the frame's two pairs of independent kernels.
+struct AuxStream {
+  void* stream;
+  void* fork[2];
+  void* join[2];
+};
+int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
+                 const AuxStream* aux = nullptr);
 
 // Persistent raster grid: SMs x resident CTAs of k_raster<TS> x waves.
 int raster_grid(int tile_shift, int waves);

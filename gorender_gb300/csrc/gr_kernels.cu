@@ -473,26 +473,54 @@ __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Set
   if (okey < a.key_cap) a.rec_of_key[okey] = r;
 }
 
-// Binning without warp aggregation (the rare clipped path).
-__device__ __forceinline__ void bin_record(const FrameArgs& a, uint32_t r, const TriRaster& t, int view) {
+// Binning without warp aggregation (the rare clipped path): up to
+// kBinDirectMax tiles directly; returns true for a triangle spanning more,
+// which the calling warp bins together (bin_tiles_warp).
+__device__ __forceinline__ bool bin_record_direct(const FrameArgs& a, uint32_t r, const TriRaster& t, int view) {
   const DevView& vw = a.views[view];
   const uint32_t tx0 = (uint32_t)t.bx0 >> a.tile_shift, tx1 = (uint32_t)t.bx1 >> a.tile_shift;
   const uint32_t ty0 = (uint32_t)t.by0 >> a.tile_shift, ty1 = (uint32_t)t.by1 >> a.tile_shift;
   const uint32_t ntiles = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
-  if (ntiles <= (uint32_t)kBinDirectMax) {
-    for (uint32_t ty = ty0; ty <= ty1; ++ty)
-      for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-        bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, a.tile_shift)), r);
-      }
-  } else {
-    const uint32_t q = atomicAdd(&a.work->nbig, 1u);
-    if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)view);
-    else atomicMax(&a.work->big_need, q + 1);
+  if (ntiles > (uint32_t)kBinDirectMax) return true;
+  for (uint32_t ty = ty0; ty <= ty1; ++ty)
+    for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+      const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
+      bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, a.tile_shift)), r);
+    }
+  return false;
+}
+
+// One warp appends record r (view `view`) to every tile its box overlaps,
+// lanes over the tiles; a narrow triangle skips tiles that one of its edges
+// excludes entirely (the exact int32 edge minimum over the tile-clipped box
+// is >= 0).  All lanes of the warp must call it with the same r.
+__device__ __forceinline__ void bin_tiles_warp(const FrameArgs& a, uint32_t r, int view) {
+  const int sh = a.tile_shift;
+  const int ts = 1 << sh;
+  const uint32_t lane = threadIdx.x & 31u;
+  const DevView& vw = a.views[view];
+  const TriRaster t = a.rast[r];
+  const uint32_t tx0 = (uint32_t)t.bx0 >> sh, tx1 = (uint32_t)t.bx1 >> sh;
+  const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
+  const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
+  const bool wide = (t.key & 0x80000000u) != 0;
+  for (uint32_t j = lane; j < n; j += 32u) {
+    const uint32_t tx = tx0 + j % nx, ty = ty0 + j / nx;
+    if (!wide) {
+      const int X0 = max((int)(tx << sh), (int)t.bx0);
+      const int X1 = min((int)(tx << sh) + ts - 1, (int)t.bx1);
+      const int Y0 = max((int)(ty << sh), (int)t.by0);
+      const int Y1 = min((int)(ty << sh) + ts - 1, (int)t.by1);
+      const int e01 = t.c01 + min(t.a01 * X0, t.a01 * X1) + min(t.b01 * Y0, t.b01 * Y1);
+      const int e12 = t.c12 + min(t.a12 * X0, t.a12 * X1) + min(t.b12 * Y0, t.b12 * Y1);
+      const int e20 = t.c20 + min(t.a20 * X0, t.a20 * X1) + min(t.b20 * Y0, t.b20 * Y1);
+      if (e01 >= 0 || e12 >= 0 || e20 >= 0) continue;
+    }
+    const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
+    bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, sh)), r);
   }
 }
 
-// Block -> item: the last item whose first block is <= blockIdx.x.
 // The item owning this block: kind 0 face blocks (k_project), 1 normal blocks
 // (k_light), 2 vertex blocks (k_vertex); the bases never decrease.
 __device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
@@ -895,6 +923,8 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
              s2 = shfl_sv(sv, lane + 2 < 9 ? lane + 2 : 0);
     const bool fan = lane + 2 < count;
     int ntpf = 0;
+    bool many = false;  // spans more than kBinDirectMax tiles: binned by the warp below
+    uint32_t rr = 0;
     if (fan && bin_test(s0, s1, s2, (float)vw.W, (float)vw.H)) {
       ntpf = 1;
       Setup s;
@@ -902,11 +932,21 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
         const uint32_t r = atomicAdd(&a.work->nrec, 1u);
         if (r < a.rec_cap) {
           write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
-          bin_record(a, r, s.r, it.view);
+          many = bin_record_direct(a, r, s.r, it.view);
+          rr = r;
         } else {
           atomicMax(&a.work->rec_need, r + 1);
         }
       }
+    }
+    // Fan triangles over many tiles, one at a time by the whole warp, so that
+    // k_clip needs nothing from k_bin_big and the two run side by side.
+    unsigned mm = __ballot_sync(FULL_MASK, many);
+    __syncwarp();  // the records just written are read by the other lanes
+    while (mm) {
+      const int l = __ffs(mm) - 1;
+      mm &= mm - 1u;
+      bin_tiles_warp(a, __shfl_sync(FULL_MASK, rr, l), it.view);
     }
     const int wt = __reduce_add_sync(FULL_MASK, ntpf);
     if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
@@ -920,38 +960,12 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
 // k_bin_big: one warp per multi-tile triangle
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
-  const int sh = a.tile_shift;
-  const int ts = 1 << sh;
   const uint32_t nbig = min(*(volatile uint32_t*)&a.work->nbig, a.big_cap);
   // one warp per queued triangle: most span 5 to a few dozen tiles
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  const uint32_t lane = threadIdx.x & 31u;
   for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nbig; q += warps) {
     const uint2 be = a.big[q];
-    const uint32_t r = be.x;
-    const DevView& vw = a.views[be.y];
-    const TriRaster t = a.rast[r];
-    const uint32_t tx0 = (uint32_t)t.bx0 >> sh, tx1 = (uint32_t)t.bx1 >> sh;
-    const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
-    const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
-    const bool wide = (t.key & 0x80000000u) != 0;
-    for (uint32_t j = lane; j < n; j += 32u) {
-      const uint32_t tx = tx0 + j % nx, ty = ty0 + j / nx;
-      if (!wide) {
-        // conservative reject: an edge that is >= 0 over the whole
-        // tile-clipped box excludes every pixel of it
-        const int X0 = max((int)(tx << sh), (int)t.bx0);
-        const int X1 = min((int)(tx << sh) + ts - 1, (int)t.bx1);
-        const int Y0 = max((int)(ty << sh), (int)t.by0);
-        const int Y1 = min((int)(ty << sh) + ts - 1, (int)t.by1);
-        const int e01 = t.c01 + min(t.a01 * X0, t.a01 * X1) + min(t.b01 * Y0, t.b01 * Y1);
-        const int e12 = t.c12 + min(t.a12 * X0, t.a12 * X1) + min(t.b12 * Y0, t.b12 * Y1);
-        const int e20 = t.c20 + min(t.a20 * X0, t.a20 * X1) + min(t.b20 * Y0, t.b20 * Y1);
-        if (e01 >= 0 || e12 >= 0 || e20 >= 0) continue;
-      }
-      const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-      bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, sh)), r);
-    }
+    bin_tiles_warp(a, be.x, (int)be.y);
   }
 }
 
@@ -1805,32 +1819,53 @@ int raster_grid(int tile_shift, int waves) {
   return max(1, sms) * max(1, per) * max(1, waves);
 }
 
-int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events) {
+int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
+                 const AuxStream* aux) {
   cudaStream_t s = (cudaStream_t)stream;
+  // Independent kernels go on two branches when an auxiliary stream is given
+  // (inside a capture the branches become parallel graph nodes): k_light
+  // beside k_vertex, k_clip beside k_bin_big.
+  cudaStream_t s2 = aux ? (cudaStream_t)aux->stream : s;
+  auto fork = [&](int k) {
+    if (!aux) return;
+    cudaEventRecord((cudaEvent_t)aux->fork[k], s);
+    cudaStreamWaitEvent(s2, (cudaEvent_t)aux->fork[k], 0);
+  };
+  auto join = [&](int k) {
+    if (!aux) return;
+    cudaEventRecord((cudaEvent_t)aux->join[k], s2);
+    cudaStreamWaitEvent(s, (cudaEvent_t)aux->join[k], 0);
+  };
   int n = 0;
   if (events) cudaEventRecord((cudaEvent_t)events[0], s);
   if (a.total_blocks > 0) {
-    if (a.light_blocks > 0) {
-      if (a.project_g == 4) k_light<4><<<a.light_blocks, 256, 0, s>>>(a);
-      else if (a.project_g == 2) k_light<2><<<a.light_blocks, 256, 0, s>>>(a);
-      else k_light<1><<<a.light_blocks, 256, 0, s>>>(a);
+    const bool light = a.light_blocks > 0;
+    if (light) {
+      fork(0);
+      if (a.project_g == 4) k_light<4><<<a.light_blocks, 256, 0, s2>>>(a);
+      else if (a.project_g == 2) k_light<2><<<a.light_blocks, 256, 0, s2>>>(a);
+      else k_light<1><<<a.light_blocks, 256, 0, s2>>>(a);
       ++n;
     }
     if (a.project_g == 4) k_vertex<4><<<a.vert_blocks, 256, 0, s>>>(a);
     else if (a.project_g == 2) k_vertex<2><<<a.vert_blocks, 256, 0, s>>>(a);
     else k_vertex<1><<<a.vert_blocks, 256, 0, s>>>(a);
     ++n;
+    if (light) join(0);
     if (a.project_g == 4) k_project<4><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     else if (a.project_g == 2) k_project<2><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     else k_project<1><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
-    if (a.flags_any & 0x01u) {
-      k_clip<<<kClipBlocks, 128, 0, s>>>(a);
+    const bool clip = a.flags_any & 0x01u;
+    if (clip) {
+      fork(1);
+      k_clip<<<kClipBlocks, 128, 0, s2>>>(a);
       ++n;
     }
     k_bin_big<<<big_blocks, 256, 0, s>>>(a);
     ++n;
+    if (clip) join(1);
     if (a.flags_any & 0xC0u) {
       k_overlay<<<big_blocks, 256, 0, s>>>(a);
       ++n;
