@@ -350,6 +350,7 @@ struct ViewIn {
   uint32_t* rgba;
   float* z;
   bool internal = false;  // may carry library-internal view flags (kViewFaceIds)
+  bool host_out = false;  // outputs in page-locked host memory (written through device addresses)
 };
 
 int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
@@ -423,7 +424,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // One view: k_raster stores the final keys and k_resolve shades every
   // pixel at full occupancy.  Many views: k_raster shades each tile (the
   // keys of a large batch would cost more memory traffic than they save).
-  const bool separate = nviews == 1;
+  // Outputs in host memory: k_raster shades each tile too, so the frame's
+  // stores cross to the host while later tiles are still rasterised instead
+  // of all at the end (measured: 0.156 against 0.173 ms a 1280x720 frame).
+  const bool separate = nviews == 1 && !views[0].host_out;
   if (separate && total_pixels > c->pkey_pixels) {
     CK(cudaStreamSynchronize(c->stream));
     dev_free(c->pkey);
@@ -716,6 +720,7 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
       if (!z) z = c->fb_z;
     }
     ViewIn v{p, rgba, z};
+    v.host_out = rgba_map || z_map;
     Prepared pr;
     if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
     if ((st = launch(c, pr.a))) return st;
