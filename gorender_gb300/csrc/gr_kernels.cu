@@ -342,6 +342,12 @@ __device__ __forceinline__ float zrec_of(float e12f, float e20f, float sumf, flo
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may be scheduled while its predecessor is still finishing;
+// it waits here, before reading anything, for the predecessor grid to
+// complete with its writes visible (a no-op after an ordinary launch).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Tile-clipped pixel box of a triangle with box [bx0,bx1] x [by0,by1] in
 // tile (tx, ty).
 __device__ __forceinline__ uint32_t tile_box(int bx0, int bx1, int by0, int by1, uint32_t tx, uint32_t ty, int sh) {
@@ -596,6 +602,7 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 // resident warps matter more than the few registers spilled.
 template <int G>
 __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs a) {
+  griddep_wait();
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
   __shared__ int s_item;
@@ -839,6 +846,7 @@ __device__ __forceinline__ SV shfl_sv(const SV& v, int src) {
 }
 
 __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
+  griddep_wait();
   const uint32_t nclip = min(*(volatile uint32_t*)&a.work->nclip, a.clip_cap);
   const int lane = (int)lane_id();
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -960,6 +968,7 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
 // k_bin_big: one warp per multi-tile triangle
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
+  griddep_wait();
   const uint32_t nbig = min(*(volatile uint32_t*)&a.work->nbig, a.big_cap);
   // one warp per queued triangle: most span 5 to a few dozen tiles
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -1646,6 +1655,7 @@ __device__ __forceinline__ void ovl_rect3(const FrameArgs& a, const DevView& vw,
 }
 
 __global__ void __launch_bounds__(256) k_overlay(const FrameArgs a) {
+  griddep_wait();
   const uint32_t n = min(*(volatile uint32_t*)&a.work->novl, a.ovl_cap);
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const Overlay o = a.ovl[q];
@@ -1679,6 +1689,7 @@ __global__ void __launch_bounds__(256) k_overlay(const FrameArgs a) {
 // reserves each part; no ordering between CTAs is needed.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
+  griddep_wait();
   __shared__ uint32_t s_nf, s_nb, s_bf, s_bb, s_max;
   const uint32_t tile = blockIdx.x * 256u + threadIdx.x;
   if (threadIdx.x == 0) {
@@ -1719,6 +1730,7 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
 // the last CTA to finish publishes and resets the frame's counters.
 template <int TS>
 __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kMinBlocks) k_raster(const FrameArgs a) {
+  griddep_wait();
   __shared__ RasterSmem<TS> sm;
   __shared__ uint32_t s_item, s_tile, s_slice, s_lastcta;
   __shared__ int s_view;
@@ -1788,6 +1800,7 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
 // that its chain of dependent loads overlaps across many warps).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
+  griddep_wait();
   const unsigned long long p = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
   if (p >= a.total_pixels) return;
   int v = 0;
@@ -1817,6 +1830,23 @@ int raster_grid(int tile_shift, int waves) {
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<32>, RasterShape<32>::kThreads, 0);
   return max(1, sms) * max(1, per) * max(1, waves);
+}
+
+// Launches kern<<<grid, block, 0, s>>>(a), after a kernel on the same stream
+// with programmatic stream serialization (the kernel waits in griddep_wait).
+template <typename K>
+static void launch_after(K kern, unsigned grid, unsigned block, cudaStream_t s, const FrameArgs& a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, a);
 }
 
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
@@ -1852,9 +1882,9 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     else k_vertex<1><<<a.vert_blocks, 256, 0, s>>>(a);
     ++n;
     if (light) join(0);
-    if (a.project_g == 4) k_project<4><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
-    else if (a.project_g == 2) k_project<2><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
-    else k_project<1><<<a.total_blocks, kProjectThreads, 0, s>>>(a);
+    if (a.project_g == 4) launch_after(k_project<4>, a.total_blocks, kProjectThreads, s, a);
+    else if (a.project_g == 2) launch_after(k_project<2>, a.total_blocks, kProjectThreads, s, a);
+    else launch_after(k_project<1>, a.total_blocks, kProjectThreads, s, a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
     const bool clip = a.flags_any & 0x01u;
@@ -1863,7 +1893,8 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
       k_clip<<<kClipBlocks, 128, 0, s2>>>(a);
       ++n;
     }
-    k_bin_big<<<big_blocks, 256, 0, s>>>(a);
+    if (events) k_bin_big<<<big_blocks, 256, 0, s>>>(a);  // timed stages: plain launches
+    else launch_after(k_bin_big, big_blocks, 256, s, a);
     ++n;
     if (clip) join(1);
     if (a.flags_any & 0xC0u) {
@@ -1875,15 +1906,14 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     cudaEventRecord((cudaEvent_t)events[1], s);
     cudaEventRecord((cudaEvent_t)events[2], s);
   }
-  k_plan<<<(a.total_tiles + 255) / 256, 256, 0, s>>>(a);
+  if (events) k_plan<<<(a.total_tiles + 255) / 256, 256, 0, s>>>(a);
+  else launch_after(k_plan, (a.total_tiles + 255) / 256, 256, s, a);
   ++n;
-  if (a.tile_shift == 4)
-    k_raster<16><<<a.raster_ctas, RasterShape<16>::kThreads, 0, s>>>(a);
-  else
-    k_raster<32><<<a.raster_ctas, RasterShape<32>::kThreads, 0, s>>>(a);
+  if (a.tile_shift == 4) launch_after(k_raster<16>, a.raster_ctas, RasterShape<16>::kThreads, s, a);
+  else launch_after(k_raster<32>, a.raster_ctas, RasterShape<32>::kThreads, s, a);
   ++n;
   if (a.pkey && a.total_pixels) {
-    k_resolve<<<(unsigned)((a.total_pixels + 255) / 256), 256, 0, s>>>(a);
+    launch_after(k_resolve, (unsigned)((a.total_pixels + 255) / 256), 256, s, a);
     ++n;
   }
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
