@@ -1684,6 +1684,11 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
       hv.Q[4 + j] = q1;
       hv.Q[8 + j] = (double)dv.mvp[12 + j];
     }
+    for (int j = 0; j < 12; ++j) {  // the same as float pairs for the float-float kernels
+      const float hi = (float)hv.Q[j];
+      hv.Qf[2 * j] = hi;
+      hv.Qf[2 * j + 1] = (float)(hv.Q[j] - (double)hi);
+    }
     pix += (uint64_t)dv.width * (uint64_t)dv.height;
     d->max_pixels = std::max(d->max_pixels, dv.width * dv.height);
     if (pix >= (1ull << 32)) st = fail(GR_ERR_UNSUPPORTED, "more than 2^32 pixels over all views");

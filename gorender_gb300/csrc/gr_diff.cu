@@ -176,24 +176,6 @@ __global__ void __launch_bounds__(kThreads) k_diff_normals(const float* __restri
   reinterpret_cast<float4*>(nhat)[n] = make_float4(v.x / len, v.y / len, v.z / len, 0.0f);
 }
 
-// Per (view, vertex): homogeneous screen x and y and clip W, in double.
-__global__ void __launch_bounds__(kThreads) k_diff_vertices(const DiffArgs a) {
-  const int i = blockIdx.x * kThreads + threadIdx.x;
-  if (i >= a.nv) return;
-  const DiffView& vw = a.views[blockIdx.y];
-  const float4 p = ldg4(a.pos + 4 * (size_t)i);
-  const double x = p.x, y = p.y, z = p.z;
-  float* o = a.vh + 6 * ((size_t)blockIdx.y * (size_t)a.nv + (size_t)i);
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const double* q = vw.Q + 4 * r;
-    const double d = __fma_rn(q[2], z, __fma_rn(q[1], y, __fma_rn(q[0], x, q[3])));
-    const float hi = (float)d;
-    o[2 * r] = hi;
-    o[2 * r + 1] = (float)(d - (double)hi);
-  }
-}
-
 // Per view: Q_0 - x Q_3 for every column x and Q_1 - y Q_3 for every row y
 // (d u / d p and d v / d p), evaluated in double and rounded to float.
 __global__ void __launch_bounds__(kThreads) k_diff_tables(const DiffArgs a) {
@@ -252,6 +234,28 @@ __device__ __forceinline__ FF ff_mul_f(FF a, float b) {
   float e = __fmaf_rn(a.hi, b, -p);
   e = __fadd_rn(e, __fmul_rn(a.lo, b));
   return fast_two_sum(p, e);
+}
+
+// Per (view, vertex): homogeneous screen x and y and clip W as float pairs,
+// Q.p formed in float-float from Q's float pairs (the products of Q's hi and
+// the float coordinates are exact with an FMA; ~48-bit significands, more
+// than the geometry needs, with no FP64 instruction).
+__global__ void __launch_bounds__(kThreads) k_diff_vertices(const DiffArgs a) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= a.nv) return;
+  const DiffView& vw = a.views[blockIdx.y];
+  const float4 p = ldg4(a.pos + 4 * (size_t)i);
+  const float c[3] = {p.x, p.y, p.z};
+  float* o = a.vh + 6 * ((size_t)blockIdx.y * (size_t)a.nv + (size_t)i);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const float* q = vw.Qf + 8 * r;
+    FF d{q[6], q[7]};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) d = ff_add(d, ff_mul_f(FF{q[2 * j], q[2 * j + 1]}, c[j]));
+    o[2 * r] = d.hi;
+    o[2 * r + 1] = d.lo;
+  }
 }
 
 // Geometry of one face at one pixel, shared by the forward and backward passes
@@ -397,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) k_diff_shade(const DiffArgs a) {
 
 // Backward: gradients of the loss of the last forward pass.
 __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
-  __shared__ double s_red[kThreads / 32];
+  __shared__ double s_red[3 * (kThreads / 32)];
   const DiffView& vw = a.views[blockIdx.y];
   const int p = blockIdx.x * kThreads + threadIdx.x;
   float gl[3] = {0.0f, 0.0f, 0.0f};
@@ -473,10 +477,25 @@ __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
       }
     }
   }
+  // light gradient: float sums within each warp, FP64 across the block's
+  // warps and blocks (one barrier)
 #pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const double t = block_sum((double)gl[j], s_red);
-    if (threadIdx.x == 0 && t != 0.0) atomicAdd(a.g_light + j, t);
+  for (int o = 16; o > 0; o >>= 1) {
+    gl[0] += __shfl_xor_sync(0xffffffffu, gl[0], o);
+    gl[1] += __shfl_xor_sync(0xffffffffu, gl[1], o);
+    gl[2] += __shfl_xor_sync(0xffffffffu, gl[2], o);
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    s_red[warp] = gl[0];
+    s_red[kThreads / 32 + warp] = gl[1];
+    s_red[2 * (kThreads / 32) + warp] = gl[2];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) t += s_red[threadIdx.x * (kThreads / 32) + w];
+    if (t != 0.0) atomicAdd(a.g_light + threadIdx.x, t);
   }
 }
 

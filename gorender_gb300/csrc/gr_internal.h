@@ -209,6 +209,7 @@ constexpr uint32_t kNoFace = 0xFFFFFFFFu;
 // One view of the differentiable object.
 struct DiffView {
   double Q[12];                     // rows 0 and 1 of S * MVP, then row 3 of MVP (clip W)
+  float Qf[24];                     // Q as float pairs: hi = float(Q), lo = float(Q - hi)
   int W, H;
   uint32_t pix_base;                // first pixel of this view in the per-pixel buffers
   uint32_t face_base;               // first global face index of this view's item
