@@ -505,14 +505,21 @@ def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):
 
 
 def cpu_baseline(scene, args):
+    import platform
     cores = os.cpu_count() or 1
     nt = min(cores, 64)
     times = _oracle_frames(scene, nt, budget_s=10.0, max_frames=200)
     med = statistics.median(times)
+    # the same restatement on one thread (a smaller bounded sample)
+    times1 = _oracle_frames(scene, 1, budget_s=6.0, max_frames=20)
+    med1 = statistics.median(times1)
     return {"value": round(scene.num_triangles / med / 1e6, 4), "unit": "Mtris/s", "cores": nt,
-            "kind": "port", "sample": f"{len(times)} full frames of {WORKLOAD}, median frame time "
+            "kind": "port", "arch": platform.machine(),
+            "sample": f"{len(times)} full frames of {WORKLOAD}, median frame time "
             f"{med * 1e3:.2f} ms (C restatement of the reference frame path, objects projected per "
-            f"task, raster in {nt} disjoint row bands)"}
+            f"task, raster in {nt} disjoint row bands)",
+            "single_thread": {"value": round(scene.num_triangles / med1 / 1e6, 4), "unit": "Mtris/s",
+                              "frames": len(times1), "median_ms": round(med1 * 1e3, 2)}}
 
 
 def run_reference(args):
