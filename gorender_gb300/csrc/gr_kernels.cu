@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(256) k_bin_big(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_raster: one CTA per TS x TS tile
+// k_raster / k_resolve: shading helpers, the per-tile raster, the resolve
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t tex_sample(const DevTex& t, float u, float v) {
   // Texture.Sample (texture.go:69-89)
@@ -1286,14 +1286,14 @@ __device__ __forceinline__ uint32_t tile_slices(const FrameArgs& a, uint32_t n, 
 template <int TS>
 struct RasterSmem {
   static constexpr int kWarps = RasterShape<TS>::kWarps;
-  static constexpr uint32_t kLargeCap = 128;  // queued wide triangles per round
+  static constexpr uint32_t kWideCap = 128;  // queued wide triangles per round
   static constexpr int kSlots = 64;           // triangle table: 32 lane slots + 32 for wide ones
   __align__(16) unsigned long long skey[TS * RasterShape<TS>::kStride];
   __align__(16) TriRaster tri[kWarps][kSlots];
   uint32_t trec[kWarps][kSlots];
   uint32_t ent[kWarps][64];
-  uint32_t large[kLargeCap + RasterShape<TS>::kThreads];
-  uint32_t next, nlarge, last;
+  uint32_t wideq[kWideCap + RasterShape<TS>::kThreads];
+  uint32_t next, nwide, last;
 };
 
 // Final colour and depth of pixel (x, y) of view vw whose visibility key is k:
@@ -1362,14 +1362,14 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   constexpr int kThreads = RasterShape<TS>::kThreads;
   constexpr int kStride = RasterShape<TS>::kStride;
   constexpr int kWarps = RasterShape<TS>::kWarps;
-  constexpr uint32_t kLargeCap = RasterSmem<TS>::kLargeCap;
+  constexpr uint32_t kWideCap = RasterSmem<TS>::kWideCap;
   unsigned long long* skey = sm.skey;
   auto& s_tri = sm.tri;
   auto& s_trec = sm.trec;
   auto& s_ent = sm.ent;
-  uint32_t* s_large = sm.large;
+  uint32_t* s_wideq = sm.wideq;
   uint32_t& s_next = sm.next;
-  uint32_t& s_nlarge = sm.nlarge;
+  uint32_t& s_nwide = sm.nwide;
   uint32_t& s_last = sm.last;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -1390,7 +1390,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   for (int i = tid; i < TS * kStride; i += kThreads) skey[i] = BG_KEY;
   if (tid == 0) {
     s_next = lo;
-    s_nlarge = 0;
+    s_nwide = 0;
   }
   __syncthreads();
 
@@ -1407,7 +1407,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     // Narrow triangles are walked by the warp that took them (span walk
     // below); int64 ("wide") triangles are queued for the whole CTA.
     for (;;) {
-      if (*(volatile uint32_t*)&s_nlarge >= kLargeCap) break;
+      if (*(volatile uint32_t*)&s_nwide >= kWideCap) break;
       uint32_t b = 0;
       if (lane == 0) b = atomicAdd(&s_next, chunk);
       b = __shfl_sync(FULL_MASK, b, 0);
@@ -1426,14 +1426,14 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       const bool live = valid && lx1 >= lx0 && ly1 >= ly0;
       const int area = live ? (lx1 - lx0 + 1) * (ly1 - ly0 + 1) : 0;
       const bool by_lane = live && !(t.key & 0x80000000u);
-      const bool large = live && !by_lane;
-      const unsigned lm = __ballot_sync(FULL_MASK, large);
+      const bool wide = live && !by_lane;
+      const unsigned lm = __ballot_sync(FULL_MASK, wide);
       if (lm) {
         uint32_t qb = 0;
         const int ldr = __ffs(lm) - 1;
-        if ((int)lane == ldr) qb = atomicAdd(&s_nlarge, (uint32_t)__popc(lm));
+        if ((int)lane == ldr) qb = atomicAdd(&s_nwide, (uint32_t)__popc(lm));
         qb = __shfl_sync(FULL_MASK, qb, ldr);
-        if (large) s_large[qb + __popc(lm & ((1u << lane) - 1u))] = r;
+        if (wide) s_wideq[qb + __popc(lm & ((1u << lane) - 1u))] = r;
       }
       if (by_lane) {
         tri[lane] = t;
@@ -1500,7 +1500,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       __syncwarp();  // lane slots are rewritten by the next chunk
     }
     __syncthreads();
-    const uint32_t nl = s_nlarge;
+    const uint32_t nl = s_nwide;
     const bool more = s_next < hi;
     // Phase 2: every warp walks the queued wide triangles and takes an
     // interleaved share of their 8x4 blocks (global block index mod warps).
@@ -1512,7 +1512,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
         // wide records with one load per lane
         q.flush(skey, a, tx0, ty0);
         if (k + lane < nl) {
-          const uint32_t r2 = s_large[k + lane];
+          const uint32_t r2 = s_wideq[k + lane];
           tri[32 + lane] = a.rast[r2];
           trec[32 + lane] = r2;
         }
@@ -1530,7 +1530,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
     q.flush(skey, a, tx0, ty0);
     __syncthreads();
     if (!more) break;
-    if (tid == 0) s_nlarge = 0;
+    if (tid == 0) s_nwide = 0;
     __syncthreads();
   }
 
