@@ -108,3 +108,21 @@ def test_soup_batch_views():
             assert np.array_equal(z.view(np.uint32), ref_z.view(np.uint32)), f"view {v}: Z differs"
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("flags", [D, D & ~gr.FRUSTUM_CLIPPING, D & ~(gr.FRUSTUM_CLIPPING | gr.BACKFACE_CULLING)],
+                         ids=["default", "no-clip", "no-clip-no-cull"])
+def test_soup_nan_inf_positions(ctx, flags):
+    """Corners at NaN and +-Inf in model space: the comparisons the reference
+    makes on them (facing test, clip planes, Go's NaN-propagating min/max in
+    the bin test, int() of NaN) decide what is drawn, bit for bit."""
+    sc = fz.soup_scene(21, 160, 120, flags, objects=1, n=600)
+    m = sc.objects[0].mesh
+    pos = m.pos.copy()
+    bad = np.arange(0, pos.shape[0], 37)
+    pos[bad[0::3], 0] = np.nan
+    pos[bad[1::3], 1] = np.inf
+    pos[bad[2::3], 2] = -np.inf
+    m = dataclasses.replace(m, pos=pos)
+    sc = dataclasses.replace(sc, objects=[dataclasses.replace(sc.objects[0], mesh=m)])
+    _check(ctx, sc)
