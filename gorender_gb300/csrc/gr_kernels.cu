@@ -374,6 +374,27 @@ __device__ __forceinline__ void bin_store(const FrameArgs& a, uint32_t tile, uin
     atomicMax(&a.work->bin_need, pos + 1);
 }
 
+// Appends record r, pixel box [bx0,bx1] x [by0,by1], to each of the at most
+// kBinDirectMax tiles [tx0,tx1] x [ty0,ty1] of view vw: every tile's
+// bin-count atomic is issued before any store, so their round trips overlap.
+__device__ __forceinline__ void bin_direct(const FrameArgs& a, const DevView& vw, uint32_t tx0, uint32_t tx1,
+                                           uint32_t ty0, uint32_t ty1, int bx0, int bx1, int by0, int by1,
+                                           uint32_t r) {
+  const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
+  uint32_t tile[kBinDirectMax], pos[kBinDirectMax];
+#pragma unroll
+  for (int k = 0; k < kBinDirectMax; ++k) {
+    if ((uint32_t)k < n) {
+      const uint32_t dy = (uint32_t)k / nx, tx = tx0 + ((uint32_t)k - dy * nx), ty = ty0 + dy;
+      tile[k] = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
+      pos[k] = bin_append(a, tile[k], tile_box(bx0, bx1, by0, by1, tx, ty, a.tile_shift));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kBinDirectMax; ++k)
+    if ((uint32_t)k < n) bin_store(a, tile[k], pos[k], r);
+}
+
 // Lighting of one normal (renderer.go:326-346): 0.5 + (normalize(W*n) . L) * 0.5
 // with Vec4.Normalize, whose length includes w.
 __device__ __forceinline__ float light_of(const float* world, V4 nrm, const float* L) {
@@ -488,11 +509,7 @@ __device__ __forceinline__ bool bin_record_direct(const FrameArgs& a, uint32_t r
   const uint32_t ty0 = (uint32_t)t.by0 >> a.tile_shift, ty1 = (uint32_t)t.by1 >> a.tile_shift;
   const uint32_t ntiles = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
   if (ntiles > (uint32_t)kBinDirectMax) return true;
-  for (uint32_t ty = ty0; ty <= ty1; ++ty)
-    for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-      const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-      bin_store(a, tile, bin_append(a, tile, tile_box(t.bx0, t.bx1, t.by0, t.by1, tx, ty, a.tile_shift)), r);
-    }
+  bin_direct(a, vw, tx0, tx1, ty0, ty1, t.bx0, t.bx1, t.by0, t.by1, r);
   return false;
 }
 
@@ -598,10 +615,12 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 // k_project: G faces a thread in the cheap pass, full warps of survivors in
 // the heavy one; everything but the general clipper.
 // ---------------------------------------------------------------------------
-// 4 CTAs per SM (64 registers a thread): the face pass is latency-bound, so
-// resident warps matter more than the few registers spilled.
+// 4 CTAs per SM (64 registers a thread) with one face a thread: the face
+// pass is latency-bound, so resident warps matter more than the few registers
+// spilled; 3 (80 registers) with more faces a thread (measured: 5 us less on
+// a 3.6 M-face frame).
 template <int G>
-__global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs a) {
+__global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(const FrameArgs a) {
   griddep_wait();
   __shared__ float s_mvp[16];
   __shared__ float s_world[16];
@@ -781,13 +800,7 @@ __global__ void __launch_bounds__(kProjectThreads, 4) k_project(const FrameArgs 
       bin_store(a, tile, pos, r);
     }
     // two to four tiles: direct appends
-    if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) {
-      for (uint32_t ty = ty0; ty <= ty1; ++ty)
-        for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-          const uint32_t tile = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
-          bin_store(a, tile, bin_append(a, tile, tile_box(pbx0, pbx1, pby0, pby1, tx, ty, a.tile_shift)), r);
-        }
-    }
+    if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) bin_direct(a, vw, tx0, tx1, ty0, ty1, pbx0, pbx1, pby0, pby1, r);
     // more: the multi-tile queue, one atomic per warp
     const bool many = ntiles > (uint32_t)kBinDirectMax;
     const unsigned mm = __ballot_sync(FULL_MASK, many);
