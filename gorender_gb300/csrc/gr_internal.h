@@ -23,6 +23,7 @@ __host__ __device__ constexpr int project_faces_per_lane(unsigned long long face
 constexpr int kBinDirectMax = 4;              // triangles spanning <= 4 tiles bin directly
 constexpr int kStageSlots = 3;                // pinned staging slots for back-to-back async draws
 constexpr int kRasterMaxSlices = 32;          // CTAs that may share one tile's bin
+static_assert(kRasterMaxSlices <= 32, "a raster work item packs its slice into 5 bits");
 constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a tile is split
 constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost

@@ -1727,6 +1727,17 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   const uint32_t count = valid ? a.bin_count[tile] : 0u;
   const uint32_t cost = valid ? count * (uint32_t)kEntryCost + a.tile_cost[tile] : 0u;
   const uint32_t ns = valid ? tile_slices(a, min(count, a.bin_cap), cost) : 0u;
+  // the tile's view (last view whose first tile <= tile), packed into the
+  // work item beside the slice so the raster CTAs do not search for it
+  int view = 0;
+  if (valid) {
+    int hi = a.num_views - 1;
+    while (view < hi) {
+      const int mid = (view + hi + 1) >> 1;
+      if (a.views[mid].tile_base <= tile) view = mid; else hi = mid - 1;
+    }
+  }
+  const uint32_t vbits = (uint32_t)view << 5;  // slices < kRasterMaxSlices = 32
   // heavy items (split tiles, or whole tiles worth half a slice) go to the
   // front of the queue so that they start first; the rest to the back
   const bool heavy = ns > 1 || cost >= a.slice_cost / 2u;
@@ -1745,9 +1756,9 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   __syncthreads();
   if (!valid) return;
   if (heavy) {
-    for (uint32_t k = 0; k < ns; ++k) a.plan[s_bf + mf + k] = make_uint2(tile, k);
+    for (uint32_t k = 0; k < ns; ++k) a.plan[s_bf + mf + k] = make_uint2(tile, k | vbits);
   } else {
-    a.plan[a.plan_cap - 1u - (s_bb + mb)] = make_uint2(tile, 0u);
+    a.plan[a.plan_cap - 1u - (s_bb + mb)] = make_uint2(tile, vbits);
   }
 }
 
@@ -1768,13 +1779,8 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
       if (i < total) {
         const uint2 w = i < front ? a.plan[i] : a.plan[a.plan_cap - 1u - (i - front)];
         s_tile = w.x;
-        s_slice = w.y;
-        int lo = 0, hi = a.num_views - 1;  // last view whose first tile <= w.x
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (a.views[mid].tile_base <= w.x) lo = mid; else hi = mid - 1;
-        }
-        s_view = lo;
+        s_slice = w.y & 31u;       // slice (kRasterMaxSlices = 32)
+        s_view = (int)(w.y >> 5);  // view, found by k_plan
       }
     }
     __syncthreads();
