@@ -29,6 +29,7 @@ constexpr int kEntryCost = 32;                // raster cost of a bin entry cove
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 constexpr int kBigBlocks = 3 * 152;           // k_bin_big / k_overlay grid (grid-stride over the queue)
+constexpr int kClearBlocks = 8 * 152;         // k_clear grid (grid-stride over the empty tiles)
 
 // Texture table entry (texture.go:19-26).
 struct DevTex {
@@ -141,6 +142,7 @@ struct DevWork {
   unsigned int plan_front, plan_back;  // raster work items: split tiles, whole tiles
   unsigned int raster_next, raster_exit;  // persistent raster: next item, finished CTAs
   unsigned int novl, ovl_need;      // overlay records written / needed
+  unsigned int nempty, clear_exit;  // empty tiles for k_clear; its finished CTAs (it resets both)
 };
 
 struct DevResult {
@@ -190,7 +192,11 @@ struct FrameArgs {
   DevResult* result;
   unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)
   unsigned long long* view_tpf_out; // per view: published by k_plan
-  uint2* plan;                      // raster work items (tile, slice), plan_cap entries
+  uint2* plan;                      // raster work items (tile, slice | view << 5), plan_cap entries
+  uint2* empty_tiles;               // (tile, view) of tiles without bin entries, shaded by k_clear
+  uint32_t empty_cap;
+  int clear_empty;                  // nonzero: tiles without bin entries go to k_clear (batches
+                                    // shaded in place), not to the raster queue
   uint32_t plan_cap;
   int raster_ctas;                  // persistent raster grid
   Overlay* ovl;                     // overlay records (views with ShowEdges / ShowVertices)
@@ -266,8 +272,8 @@ int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start
 // the frame's two pairs of independent kernels.
 struct AuxStream {
   void* stream;
-  void* fork[2];
-  void* join[2];
+  void* fork[3];
+  void* join[3];
 };
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
                  const AuxStream* aux = nullptr);

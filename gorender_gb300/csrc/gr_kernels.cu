@@ -1715,11 +1715,12 @@ __global__ void __launch_bounds__(256) k_overlay(const FrameArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   griddep_wait();
-  __shared__ uint32_t s_nf, s_nb, s_bf, s_bb, s_max;
+  __shared__ uint32_t s_nf, s_nb, s_ne, s_bf, s_bb, s_be, s_max;
   const uint32_t tile = blockIdx.x * 256u + threadIdx.x;
   if (threadIdx.x == 0) {
     s_nf = 0;
     s_nb = 0;
+    s_ne = 0;
     s_max = 0;
   }
   __syncthreads();
@@ -1741,21 +1742,28 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   // heavy items (split tiles, or whole tiles worth half a slice) go to the
   // front of the queue so that they start first; the rest to the back
   const bool heavy = ns > 1 || cost >= a.slice_cost / 2u;
-  uint32_t mf = 0, mb = 0;
+  // A tile without bin entries of a batch shaded in place goes to k_clear's
+  // list instead of the raster queue: all background, no keys.
+  const bool clear = count == 0 && a.clear_empty;
+  uint32_t mf = 0, mb = 0, me = 0;
   if (valid) {
     atomicMax(&s_max, count);
-    if (heavy) mf = atomicAdd(&s_nf, ns);
+    if (clear) me = atomicAdd(&s_ne, 1u);
+    else if (heavy) mf = atomicAdd(&s_nf, ns);
     else mb = atomicAdd(&s_nb, 1u);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     s_bf = s_nf ? atomicAdd(&a.work->plan_front, s_nf) : 0u;
     s_bb = s_nb ? atomicAdd(&a.work->plan_back, s_nb) : 0u;
+    s_be = s_ne ? atomicAdd(&a.work->nempty, s_ne) : 0u;
     if (s_max) atomicMax(&a.work->max_bin, s_max);
   }
   __syncthreads();
   if (!valid) return;
-  if (heavy) {
+  if (clear) {
+    if (s_be + me < a.empty_cap) a.empty_tiles[s_be + me] = make_uint2(tile, (uint32_t)view);
+  } else if (heavy) {
     for (uint32_t k = 0; k < ns; ++k) a.plan[s_bf + mf + k] = make_uint2(tile, k | vbits);
   } else {
     a.plan[a.plan_cap - 1u - (s_bb + mb)] = make_uint2(tile, vbits);
@@ -1852,6 +1860,59 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
   vw.out_z[o] = z;
 }
 
+// ---------------------------------------------------------------------------
+// k_clear: the tiles without bin entries of frames shaded in place (k_plan's
+// list), four pixels a thread over all of them, beside k_raster: Clear and
+// DotGrid (rasterizer.go:36-52), overlay marks, crosshair and fog through
+// resolve_pixel with the background key.  The last CTA to finish returns the
+// list's counter to zero for the next frame.
+// ---------------------------------------------------------------------------
+template <int TS>
+__global__ void __launch_bounds__(256) k_clear(const FrameArgs a) {
+  __shared__ uint32_t s_last;
+  constexpr uint32_t kQuads = TS * TS / 4;  // four-pixel groups a tile
+  const uint32_t ne = min(*(volatile uint32_t*)&a.work->nempty, a.empty_cap);
+  const unsigned long long total = (unsigned long long)ne * kQuads;
+  for (unsigned long long q = (unsigned long long)blockIdx.x * 256u + threadIdx.x; q < total;
+       q += (unsigned long long)gridDim.x * 256u) {
+    const uint2 e = a.empty_tiles[q / kQuads];
+    const uint32_t qq = (uint32_t)(q % kQuads);
+    const DevView& vw = a.views[e.y];
+    const uint32_t lt = e.x - vw.tile_base;
+    const int x = (int)(lt % (uint32_t)vw.tiles_x) * TS + (int)(qq % (TS / 4)) * 4;
+    const int y = (int)(lt / (uint32_t)vw.tiles_x) * TS + (int)(qq / (TS / 4));
+    if (y >= vw.H) continue;
+    uint32_t c[4];
+    float z[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      c[j] = 0u;
+      z[j] = 0.0f;
+      if (x + j < vw.W) resolve_pixel(a, vw, x + j, y, BG_KEY, c[j], z[j]);
+    }
+    const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
+    if (vw.vec_ok && x + 3 < vw.W) {
+      *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(c[0], c[1], c[2], c[3]);
+      *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(z[0], z[1], z[2], z[3]);
+    } else {
+      for (int j = 0; j < 4 && x + j < vw.W; ++j) {
+        vw.out_rgba[o + j] = c[j];
+        vw.out_z[o + j] = z[j];
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&a.work->clear_exit, 1u) == gridDim.x - 1 ? 1u : 0u;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    a.work->nempty = 0u;
+    a.work->clear_exit = 0u;
+  }
+}
+
 int raster_grid(int tile_shift, int waves) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
@@ -1940,6 +2001,13 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
   if (events) k_plan<<<(a.total_tiles + 255) / 256, 256, 0, s>>>(a);
   else launch_after(k_plan, (a.total_tiles + 255) / 256, 256, s, a);
   ++n;
+  const bool clear = a.clear_empty;  // tiles without bin entries, shaded in place by k_clear
+  if (clear) {
+    fork(2);
+    if (a.tile_shift == 4) k_clear<16><<<kClearBlocks, 256, 0, s2>>>(a);
+    else k_clear<32><<<kClearBlocks, 256, 0, s2>>>(a);
+    ++n;
+  }
   if (a.tile_shift == 4) launch_after(k_raster<16>, a.raster_ctas, RasterShape<16>::kThreads, s, a);
   else launch_after(k_raster<32>, a.raster_ctas, RasterShape<32>::kThreads, s, a);
   ++n;
@@ -1947,6 +2015,7 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     launch_after(k_resolve, (unsigned)((a.total_pixels + 255) / 256), 256, s, a);
     ++n;
   }
+  if (clear) join(2);
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
   if (launches) *launches = n;
   return (int)cudaGetLastError();

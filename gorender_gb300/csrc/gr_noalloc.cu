@@ -57,7 +57,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
-  size_t items, texs, views, view_tpf, view_tpf_out, plan, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip,
+  size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip,
       vlight, vclip, vscr, gkey, tile_done, work, result, end;
 };
 
@@ -70,6 +70,7 @@ constexpr Layout make_layout() {
   l.view_tpf = o; o += up256(sizeof(unsigned long long));
   l.view_tpf_out = o; o += up256(sizeof(unsigned long long));
   l.plan = o; o += up256(sizeof(uint2) * kTiles * kRasterMaxSlices);
+  l.empty = o; o += up256(sizeof(uint2) * kTiles);
   l.rast = o; o += up256(sizeof(TriRaster) * kRecCap);
   l.shade = o; o += up256(sizeof(TriShade) * kRecCap);
   l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
@@ -271,6 +272,8 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.view_tpf_out = (unsigned long long*)(base + kLayout.view_tpf_out);
   a.plan = (uint2*)(base + kLayout.plan);
   a.plan_cap = (uint32_t)(kTiles * kRasterMaxSlices);
+  a.empty_tiles = (uint2*)(base + kLayout.empty);
+  a.empty_cap = (uint32_t)kTiles;
   a.raster_ctas = raster_grid(5, 1);
 
   // The array keeps the previous call's contents: zero what the kernels
