@@ -383,14 +383,6 @@ int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
     if (st) return st;
     c->plan_cap = (uint32_t)want_plan;
   }
-  if (tiles > c->empty_cap) {
-    CK(cudaStreamSynchronize(c->stream));
-    dev_free(c->empty_tiles);
-    c->empty_cap = 0;
-    int32_t st = dev_alloc(&c->empty_tiles, tiles);
-    if (st) return st;
-    c->empty_cap = tiles;
-  }
   return GR_OK;
 }
 
@@ -608,8 +600,6 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.view_tpf_out = c->view_tpf_out;
   a.plan = c->plan;
   a.plan_cap = c->plan_cap;
-  a.empty_tiles = c->empty_tiles;
-  a.empty_cap = c->empty_cap;
   a.raster_ctas = raster_grid(c->tile_shift, c->raster_waves);
   a.ovl = c->ovl;
   a.ovl_cap = c->ovl_cap;
@@ -620,6 +610,15 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // batch 1.81 -> 1.62 ms); one view keeps them in the raster queue, where
   // they cost less than k_clear's launch (0.153 against 0.166 ms a frame).
   a.clear_empty = (!separate && nviews > 1) ? 1 : 0;
+  if (a.clear_empty && total_tiles > c->empty_cap) {  // allocated only for such frames
+    CK(cudaStreamSynchronize(c->stream));
+    dev_free(c->empty_tiles);
+    c->empty_cap = 0;
+    if ((st = dev_alloc(&c->empty_tiles, (size_t)total_tiles))) return st;
+    c->empty_cap = total_tiles;
+  }
+  a.empty_tiles = c->empty_tiles;
+  a.empty_cap = c->empty_cap;
   a.total_pixels = total_pixels;
   out.faces = faces;
   out.nitems = live;
