@@ -1585,6 +1585,7 @@ struct gr_diff {
   float* bbox_partial = nullptr;        // kBBoxBlocks x 6
   unsigned* bbox_done = nullptr;
   double* d_acc = nullptr;              // loss, light gradient x 3
+  double* d_partials = nullptr;         // per-warp sums (kDiffSlots x 4), zero when idle
   double* h_acc = nullptr;              // pinned
   gr_diff_params last{};                // parameters of the last forward
   const float* last_target = nullptr;
@@ -1618,6 +1619,7 @@ DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* targe
   a.target = target;
   a.loss = d->d_acc;
   a.g_light = d->d_acc + 1;
+  a.partials = d->d_partials;
   return a;
 }
 
@@ -1627,6 +1629,7 @@ void diff_free(gr_diff* d) {
   dev_free(d->vh); dev_free(d->col_tab); dev_free(d->row_tab);
   dev_free(d->bbox_partial); dev_free(d->bbox_done);
   dev_free(d->d_acc);
+  dev_free(d->d_partials);
   if (d->h_acc) cudaFreeHost(d->h_acc);
   d->h_acc = nullptr;
 }
@@ -1727,6 +1730,9 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st && cudaMemsetAsync(d->bbox_done, 0, sizeof(unsigned), c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff counters");
   if (!st) st = dev_alloc(&d->d_acc, (size_t)4);
+  if (!st) st = dev_alloc(&d->d_partials, (size_t)kDiffSlots * 4);
+  if (!st && cudaMemsetAsync(d->d_partials, 0, sizeof(double) * kDiffSlots * 4, c->stream) != cudaSuccess)
+    st = fail(GR_ERR_CUDA, "diff partials");
   if (!st && cudaMallocHost((void**)&d->h_acc, 4 * sizeof(double)) != cudaSuccess) {
     d->h_acc = nullptr;
     st = fail(GR_ERR_OUT_OF_MEMORY, "pinned accumulator");

@@ -341,24 +341,14 @@ __device__ __forceinline__ int wrap_index(float u, int n) {
   return i < 0 ? i + n : i;
 }
 
-// Block-wide sum of one double; thread 0 gets the result.
-__device__ __forceinline__ double block_sum(double v, double* s_red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) s_red[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (warp == 0) {
-    t = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  }
-  __syncthreads();
-  return t;
+// The calling warp's slot of DiffArgs::partials (warps spread over the slots
+// so that their atomics rarely meet).
+__device__ __forceinline__ int diff_slot() {
+  return (int)(((blockIdx.y * gridDim.x + blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5)) & (kDiffSlots - 1));
 }
 
 // Forward: per pixel record, shaded pixel and the loss.  Grid (pixels/256, views).
 __global__ void __launch_bounds__(kThreads) k_diff_shade(const DiffArgs a) {
-  __shared__ double s_red[kThreads / 32];
   const DiffView& vw = a.views[blockIdx.y];
   const int p = blockIdx.x * kThreads + threadIdx.x;
   float lp = 0.0f;
@@ -395,13 +385,16 @@ __global__ void __launch_bounds__(kThreads) k_diff_shade(const DiffArgs a) {
     const float dx = out.x - tg.x, dy = out.y - tg.y, dz = out.z - tg.z, dw = out.w - tg.w;
     lp = dx * dx + dy * dy + dz * dz + dw * dw;
   }
-  const double t = block_sum((double)lp, s_red);
-  if (threadIdx.x == 0 && t != 0.0) atomicAdd(a.loss, t);
+  // the loss in FP64: within the warp, then one atomic into the warp's slot
+  // (k_diff_sum adds the slots up), so warps never wait for each other
+  double t = (double)lp;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0 && t != 0.0) atomicAdd(a.partials + 4 * diff_slot(), t);
 }
 
 // Backward: gradients of the loss of the last forward pass.
 __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
-  __shared__ double s_red[3 * (kThreads / 32)];
   const DiffView& vw = a.views[blockIdx.y];
   const int p = blockIdx.x * kThreads + threadIdx.x;
   float gl[3] = {0.0f, 0.0f, 0.0f};
@@ -477,25 +470,40 @@ __global__ void __launch_bounds__(kThreads) k_diff_grad(const DiffArgs a) {
       }
     }
   }
-  // light gradient: float sums within each warp, FP64 across the block's
-  // warps and blocks (one barrier)
+  // light gradient: float sums within the warp, then FP64 atomics into the
+  // warp's slot (k_diff_sum adds the slots up)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     gl[0] += __shfl_xor_sync(0xffffffffu, gl[0], o);
     gl[1] += __shfl_xor_sync(0xffffffffu, gl[1], o);
     gl[2] += __shfl_xor_sync(0xffffffffu, gl[2], o);
   }
-  const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    s_red[warp] = gl[0];
-    s_red[kThreads / 32 + warp] = gl[1];
-    s_red[2 * (kThreads / 32) + warp] = gl[2];
+    double* p = a.partials + 4 * diff_slot();
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (gl[j] != 0.0f) atomicAdd(p + 1 + j, (double)gl[j]);
   }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    double t = 0.0;
-    for (int w = 0; w < kThreads / 32; ++w) t += s_red[threadIdx.x * (kThreads / 32) + w];
-    if (t != 0.0) atomicAdd(a.g_light + threadIdx.x, t);
+}
+
+// Adds components [c0, c0 + n) of the per-warp slots into dst[0 .. n) and
+// returns the slots to zero.  One block of kDiffSlots threads.
+__global__ void __launch_bounds__(kDiffSlots) k_diff_sum(const DiffArgs a, int c0, int n, double* dst) {
+  __shared__ double s_w[kDiffSlots / 32];
+  for (int j = 0; j < n; ++j) {
+    double* p = a.partials + 4 * threadIdx.x + c0 + j;
+    double t = *p;
+    *p = 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sum = 0.0;
+      for (int w = 0; w < kDiffSlots / 32; ++w) sum += s_w[w];
+      dst[j] += sum;
+    }
+    __syncthreads();
   }
 }
 
@@ -521,12 +529,14 @@ int launch_diff_forward(const DiffArgs& a, int max_side, void* stream) {
   k_diff_tables<<<dim3((unsigned)((max_side + kThreads - 1) / kThreads), (unsigned)a.num_views), kThreads, 0, s>>>(a);
   const dim3 grid((unsigned)((a.max_pixels + kThreads - 1) / kThreads), (unsigned)a.num_views);
   k_diff_shade<<<grid, kThreads, 0, s>>>(a);
+  k_diff_sum<<<1, kDiffSlots, 0, s>>>(a, 0, 1, a.loss);
   return (int)cudaGetLastError();
 }
 
 int launch_diff_backward(const DiffArgs& a, void* stream) {
   const dim3 grid((unsigned)((a.max_pixels + kThreads - 1) / kThreads), (unsigned)a.num_views);
   k_diff_grad<<<grid, kThreads, 0, (cudaStream_t)stream>>>(a);
+  k_diff_sum<<<1, kDiffSlots, 0, (cudaStream_t)stream>>>(a, 1, 3, a.g_light);
   return (int)cudaGetLastError();
 }
 

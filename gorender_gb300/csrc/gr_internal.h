@@ -259,7 +259,9 @@ struct DiffArgs {
   float* g_vcol;                    // nv x 3
   float* g_tex;                     // th x tw x 4
   double* g_light;                  // 3, accumulated
+  double* partials;                 // kDiffSlots x {loss, light x, y, z}: per-warp sums, zero when idle
 };
+constexpr int kDiffSlots = 1024;     // slots of DiffArgs::partials
 
 // FrameBuffer.Fog on one framebuffer (gr_kernels.cu).
 int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start, float fog_end, uint32_t color,
