@@ -1586,6 +1586,7 @@ struct gr_diff {
   unsigned* bbox_done = nullptr;
   double* d_acc = nullptr;              // loss, light gradient x 3
   double* d_partials = nullptr;         // per-warp sums (kDiffSlots x 4), zero when idle
+  float* d_gface = nullptr;             // per-face corner gradient sums (nf x 18), zero when idle
   double* h_acc = nullptr;              // pinned
   gr_diff_params last{};                // parameters of the last forward
   const float* last_target = nullptr;
@@ -1620,6 +1621,7 @@ DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* targe
   a.loss = d->d_acc;
   a.g_light = d->d_acc + 1;
   a.partials = d->d_partials;
+  a.g_face = d->d_gface;
   return a;
 }
 
@@ -1630,6 +1632,7 @@ void diff_free(gr_diff* d) {
   dev_free(d->bbox_partial); dev_free(d->bbox_done);
   dev_free(d->d_acc);
   dev_free(d->d_partials);
+  dev_free(d->d_gface);
   if (d->h_acc) cudaFreeHost(d->h_acc);
   d->h_acc = nullptr;
 }
@@ -1733,6 +1736,9 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st) st = dev_alloc(&d->d_partials, (size_t)kDiffSlots * 4);
   if (!st && cudaMemsetAsync(d->d_partials, 0, sizeof(double) * kDiffSlots * 4, c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff partials");
+  if (!st) st = dev_alloc(&d->d_gface, (size_t)d->nf * 18);
+  if (!st && cudaMemsetAsync(d->d_gface, 0, sizeof(float) * 18 * (size_t)d->nf, c->stream) != cudaSuccess)
+    st = fail(GR_ERR_CUDA, "diff face sums");
   if (!st && cudaMallocHost((void**)&d->h_acc, 4 * sizeof(double)) != cudaSuccess) {
     d->h_acc = nullptr;
     st = fail(GR_ERR_OUT_OF_MEMORY, "pinned accumulator");
