@@ -208,7 +208,8 @@ struct FrameArgs {
 };
 
 // View flag (internal, never set by callers): the raster resolve writes the
-// winning face's global index (or kNoFace) into out_rgba instead of a colour.
+// winning face's global index (or kNoFace) into out_rgba instead of a colour,
+// computed from the visibility key alone, and writes no depth.
 constexpr uint32_t kViewFaceIds = 0x80000000u;
 constexpr uint32_t kNoFace = 0xFFFFFFFFu;
 

@@ -1330,6 +1330,11 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
     out_z = -1.0f;
   } else {
     const uint32_t okey = (uint32_t)k & 0x7FFFFFFFu;
+    if (face_ids) {  // the face of order key face * 8 + fan + 1; no depth is output
+      out_c = (okey - 1u) / (uint32_t)kKeysPerFace;
+      out_z = 0.0f;
+      return;
+    }
     const uint32_t r = a.rec_of_key[okey];
     const TriRaster t = a.rast[r];
     bool inside;
@@ -1337,10 +1342,6 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
     edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
     const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
     out_z = z;
-    if (face_ids) {
-      out_c = (okey - 1u) / (uint32_t)kKeysPerFace;  // the face of order key face * 8 + fan + 1
-      return;
-    }
     const TriShade s = a.shade[r];
     const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
     uint32_t c;
@@ -1610,13 +1611,14 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       }
       const int x = tx0 + col;
       const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
+      const bool with_z = !(vw.flags & kViewFaceIds);  // face-id views output no depth
       if (vw.vec_ok && x + 3 <= tx1) {
         *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(out_c[0], out_c[1], out_c[2], out_c[3]);
-        *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
+        if (with_z) *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(out_z[0], out_z[1], out_z[2], out_z[3]);
       } else {
         for (int j = 0; j < 4 && x + j <= tx1; ++j) {
           vw.out_rgba[o + j] = out_c[j];
-          vw.out_z[o + j] = out_z[j];
+          if (with_z) vw.out_z[o + j] = out_z[j];
         }
       }
     }
@@ -1857,7 +1859,7 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
   float z;
   resolve_pixel(a, vw, x, y, a.pkey[p], c, z);
   vw.out_rgba[o] = c;
-  vw.out_z[o] = z;
+  if (!(vw.flags & kViewFaceIds)) vw.out_z[o] = z;  // face-id views output no depth
 }
 
 // ---------------------------------------------------------------------------
@@ -1891,13 +1893,14 @@ __global__ void __launch_bounds__(256) k_clear(const FrameArgs a) {
       if (x + j < vw.W) resolve_pixel(a, vw, x + j, y, BG_KEY, c[j], z[j]);
     }
     const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
+    const bool with_z = !(vw.flags & kViewFaceIds);  // face-id views output no depth
     if (vw.vec_ok && x + 3 < vw.W) {
       *reinterpret_cast<uint4*>(vw.out_rgba + o) = make_uint4(c[0], c[1], c[2], c[3]);
-      *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(z[0], z[1], z[2], z[3]);
+      if (with_z) *reinterpret_cast<float4*>(vw.out_z + o) = make_float4(z[0], z[1], z[2], z[3]);
     } else {
       for (int j = 0; j < 4 && x + j < vw.W; ++j) {
         vw.out_rgba[o + j] = c[j];
-        vw.out_z[o + j] = z[j];
+        if (with_z) vw.out_z[o + j] = z[j];
       }
     }
   }
