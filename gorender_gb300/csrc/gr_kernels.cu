@@ -1886,11 +1886,24 @@ __global__ void __launch_bounds__(256) k_clear(const FrameArgs a) {
     if (y >= vw.H) continue;
     uint32_t c[4];
     float z[4];
+    if (!(vw.flags & (0xC0u | 0x100u | kViewFaceIds)) && !vw.fog_on) {
+      // plain background: Clear, and DotGrid at x, y multiples of 10 from 10
+      // on (the same values resolve_pixel gives with these flags)
+      const bool dot_row = y >= 10 && y % 10 == 0;
+      const int xr = x % 10;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      c[j] = 0u;
-      z[j] = 0.0f;
-      if (x + j < vw.W) resolve_pixel(a, vw, x + j, y, BG_KEY, c[j], z[j]);
+      for (int j = 0; j < 4; ++j) {
+        const bool dot = dot_row && x + j >= 10 && (xr + j == 0 || xr + j == 10);
+        c[j] = dot ? 0xFF646464u : 0xFF323232u;
+        z[j] = -1.0f;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        c[j] = 0u;
+        z[j] = 0.0f;
+        if (x + j < vw.W) resolve_pixel(a, vw, x + j, y, BG_KEY, c[j], z[j]);
+      }
     }
     const size_t o = (size_t)y * (size_t)vw.W + (size_t)x;
     const bool with_z = !(vw.flags & kViewFaceIds);  // face-id views output no depth
