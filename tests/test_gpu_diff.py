@@ -133,3 +133,16 @@ def test_full_size_workload(oracle_lib):
         _compare(run)
     finally:
         run.close()
+
+
+def test_single_view(oracle_lib):
+    """One view: its visibility pass goes through the per-pixel resolve
+    kernel (face ids from the keys) instead of the in-place tile resolve."""
+    run = Run(dc.small_case(views=1, size=128, level=4, tex_size=32, seed=7))
+    try:
+        ref = dc.oracle_ids(run.sc)
+        assert (ref != dc.NO_FACE).sum() > 500
+        assert np.array_equal(run.ids, ref)
+        _compare(run)
+    finally:
+        run.close()
