@@ -197,9 +197,10 @@ def run_ours(args):
         kms += np.array(buf[:])
         ctx.flush_l2()
     kms /= kprof
-    # the profiled pass brackets three stages: k_light + k_vertex + k_project |
-    # k_clip + k_bin_big | k_plan + k_raster + k_resolve (k_plan is a
-    # one-thread-per-tile scan; k_resolve shades the one view's pixels)
+    # the profiled pass brackets three stages: k_light + k_vertex + k_cull +
+    # k_setup (k_clip starts beside k_setup) | k_bin_big and the rest of
+    # k_clip | k_plan + k_raster + k_resolve (k_plan is a one-thread-per-tile
+    # scan; k_resolve shades the one view's pixels)
     names = ["project_stage", "bin_stage", "raster_stage"]
     top = int(np.argmax(kms))
     ab = algorithmic_bytes(scene)
@@ -261,8 +262,8 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(top_bytes),
                      "kernel_ms": {nm: round(float(v), 5) for nm, v in zip(names, kms)},
-                     "stages": {"project_stage": "k_light + k_vertex + k_project",
-                                "bin_stage": "k_clip + k_bin_big",
+                     "stages": {"project_stage": "k_light + k_vertex + k_cull + k_setup",
+                                "bin_stage": "k_bin_big + the rest of k_clip (which starts beside k_setup)",
                                 "raster_stage": "k_plan + k_raster + k_resolve"},
                      "frame_algorithmic_bytes": int(ab["frame"])},
         "gpu_launches": int(launches_per_frame * args.steps),

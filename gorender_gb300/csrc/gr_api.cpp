@@ -113,6 +113,8 @@ struct gr_context {
   uint32_t gkey_tiles = 0;
   uint2* clip = nullptr;            // faces for the general clipper
   uint32_t clip_cap = 0;
+  uint2* kept = nullptr;         // faces k_cull kept whole (one entry per face of the frame)
+  uint32_t kept_cap = 0;
   float* vlight = nullptr;          // per-normal Gouraud intensities
   uint64_t vlight_cap = 0;
   float4* vclip = nullptr;          // per item vertex: clip position and screen x, y (k_vertex)
@@ -296,6 +298,14 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
     c->clip_cap = 0;
     if ((st = dev_alloc(&c->clip, want_clip))) return st;
     c->clip_cap = (uint32_t)want_clip;
+  }
+  if (faces > c->kept_cap) {  // every face may be kept: sized to the frame, never overflows
+    if ((st = sync())) return st;
+    dev_free(c->kept);
+    c->kept_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(faces, 1024);
+    if ((st = dev_alloc(&c->kept, cap))) return st;
+    c->kept_cap = (uint32_t)cap;
   }
   uint64_t want_big = std::max<uint64_t>(c->want_big_cap, faces / 8 + 1024);
   if (want_big > c->big_cap) {
@@ -589,6 +599,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.slice_cost = c->slice_cost;
   a.clip = c->clip;
   a.clip_cap = c->clip_cap;
+  a.kept = c->kept;
+  a.kept_cap = c->kept_cap;
+  a.setup_blocks = (int)std::min<uint64_t>(kSetupBlocks, (faces + kProjectThreads - 1) / kProjectThreads);
   a.vlight = c->vlight;
   a.light_blocks = light_blocks;
   a.vclip = c->vclip;
@@ -677,7 +690,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
 uint64_t buffers_signature(const gr_context* c) {
   const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->wide, (uintptr_t)c->tcol,
                           (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->gkey,
-                          (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->big, (uintptr_t)c->vlight,
+                          (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->kept, c->kept_cap, (uintptr_t)c->big, (uintptr_t)c->vlight,
                           (uintptr_t)c->vclip, (uintptr_t)c->vscr,
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, (uintptr_t)c->empty_tiles, c->empty_cap, c->rec_cap, c->key_cap, c->bin_cap,
@@ -833,7 +846,7 @@ int32_t gr_context_destroy(gr_context* c) {
   if (c->h_items) cudaFreeHost(c->h_items);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
-  dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->vlight);
+  dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->kept); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);
   dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan); dev_free(c->empty_tiles);
   dev_free(c->ovl); dev_free(c->ovl_key); dev_free(c->pkey);

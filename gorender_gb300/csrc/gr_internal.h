@@ -15,8 +15,8 @@ constexpr int kNarrowLimit = 16384;           // |screen coordinate| < 2^14 => i
 constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes fans into <= 7
 constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
 constexpr int kProjectThreads = 256;
-// k_project: faces a thread tests before the survivors are compacted (1, 2
-// or 4, by the frame's face count: enough blocks to fill the GPU first)
+// k_cull (and k_vertex / k_light): faces (vertices, normals) a thread, 1, 2
+// or 4 by the frame's face count
 __host__ __device__ constexpr int project_faces_per_lane(unsigned long long faces) {
   return faces >= 2000000ull ? 4 : faces >= 1000000ull ? 2 : 1;
 }
@@ -27,6 +27,8 @@ static_assert(kRasterMaxSlices <= 32, "a raster work item packs its slice into 5
 constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a tile is split
 constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
+constexpr int kSetupCtasPerSm = 2;            // k_setup: resident CTAs an SM (128 registers a thread)
+constexpr int kSetupBlocks = kSetupCtasPerSm * 152;  // k_setup grid (grid-stride over the kept faces)
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 constexpr int kBigBlocks = 3 * 152;           // k_bin_big / k_overlay grid (grid-stride over the queue)
 constexpr int kClearBlocks = 8 * 152;         // k_clear grid (grid-stride over the empty tiles)
@@ -74,7 +76,7 @@ struct DevItem {
   const float* vcol;                // nv x 3 (may be null)
   int nv, nn, nf;
   uint32_t face_base;               // global face order of face 0
-  int block_base;                   // first k_project block of this item
+  int block_base;                   // first k_cull block of this item
   int light_base;                   // first entry of this item in FrameArgs::vlight
   int light_block_base;             // first k_light block of this item
   int view;                         // index into FrameArgs::views
@@ -143,6 +145,7 @@ struct DevWork {
   unsigned int raster_next, raster_exit;  // persistent raster: next item, finished CTAs
   unsigned int novl, ovl_need;      // overlay records written / needed
   unsigned int nempty, clear_exit;  // empty tiles for k_clear; its finished CTAs (it resets both)
+  unsigned int nkept;               // faces k_cull kept whole, for k_setup
 };
 
 struct DevResult {
@@ -160,7 +163,7 @@ struct FrameArgs {
   int tile_shift;                   // raster tile = (1 << tile_shift)^2 pixels (4 or 5)
   int num_items;
   int total_blocks;
-  int project_g;                    // k_project faces a thread (project_faces_per_lane); k_light and
+  int project_g;                    // k_cull faces a thread (project_faces_per_lane); k_light and
                                     // k_vertex take as many normals / vertices a thread
   uint32_t bin_cap;
   uint32_t rec_cap;
@@ -180,6 +183,10 @@ struct FrameArgs {
   uint2* big;                       // multi-tile queue: (record, view)
   uint2* clip;                      // (item, face) pairs for the general clipper
   uint32_t clip_cap;
+  uint2* kept;                      // (item, face) of the faces k_cull kept whole; k_setup writes
+                                    // the record of entry k as record k
+  uint32_t kept_cap;                // >= the frame's faces: never overflows
+  int setup_blocks;                 // k_setup grid
   float* vlight;                    // per-normal Gouraud intensities (k_light)
   int light_blocks;                 // k_light grid (0: no Gouraud item)
   float4* vclip;                    // per item vertex: clip-space position (k_vertex)
@@ -271,8 +278,8 @@ int launch_fog(uint32_t* rgba, const float* z, long long pixels, float fog_start
                void* stream);
 
 // Kernel launchers (gr_kernels.cu).
-// events (optional): 4 cudaEvent_t recorded before k_project, after k_project,
-// after k_bin_big and after k_raster.
+// events (optional): 4 cudaEvent_t recorded before k_vertex, after k_setup,
+// after k_bin_big (and k_clip) and after k_raster.
 // A second stream and its fork / join events (created with timing off) for
 // the frame's two pairs of independent kernels.
 struct AuxStream {

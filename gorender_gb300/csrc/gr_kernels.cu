@@ -4,13 +4,14 @@
 // into a CUDA graph and replayed):
 //   k_light    Gouraud intensity once per vertex normal.
 //   k_vertex   clip-space position and unsnapped screen x, y once per vertex.
-//   k_project  faces in groups of 32 x G per warp: backface and frustum tests
-//              on every face, survivors compacted, then for full warps of
-//              survivors the attributes, screen vertices, bin test (TPF) and
-//              edge-function setup; records are appended with one atomic per
-//              warp and binned with warp-aggregated atomics (__match_any_sync)
-//              or, past four tiles, queued for k_bin_big.  Straddling faces
-//              go to k_clip (the general clipper, one warp per face).
+//   k_cull     faces in groups of 32 x G per warp: backface and frustum
+//              tests on every face; faces kept whole are compacted into one
+//              list, straddling faces go to k_clip (the general clipper, one
+//              warp per face, beside k_setup).
+//   k_setup    full warps of kept faces: attributes, screen vertices, bin
+//              test (TPF) and edge-function setup; records are appended with
+//              one atomic per warp and binned with warp-aggregated atomics
+//              (__match_any_sync) or, past four tiles, queued for k_bin_big.
 //   k_bin_big  one warp per multi-tile triangle: appends it to every tile its
 //              edge functions can reach.
 //   k_plan     splits heavy tiles into slices by estimated cost and orders
@@ -377,16 +378,16 @@ __device__ __forceinline__ void bin_store(const FrameArgs& a, uint32_t tile, uin
 // Appends record r, pixel box [bx0,bx1] x [by0,by1], to each of the at most
 // kBinDirectMax tiles [tx0,tx1] x [ty0,ty1] of view vw: every tile's
 // bin-count atomic is issued before any store, so their round trips overlap.
-__device__ __forceinline__ void bin_direct(const FrameArgs& a, const DevView& vw, uint32_t tx0, uint32_t tx1,
-                                           uint32_t ty0, uint32_t ty1, int bx0, int bx1, int by0, int by1,
-                                           uint32_t r) {
+__device__ __forceinline__ void bin_direct(const FrameArgs& a, uint32_t tile_base, uint32_t tiles_x, uint32_t tx0,
+                                           uint32_t tx1, uint32_t ty0, uint32_t ty1, int bx0, int bx1, int by0,
+                                           int by1, uint32_t r) {
   const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
   uint32_t tile[kBinDirectMax], pos[kBinDirectMax];
 #pragma unroll
   for (int k = 0; k < kBinDirectMax; ++k) {
     if ((uint32_t)k < n) {
       const uint32_t dy = (uint32_t)k / nx, tx = tx0 + ((uint32_t)k - dy * nx), ty = ty0 + dy;
-      tile[k] = vw.tile_base + ty * (uint32_t)vw.tiles_x + tx;
+      tile[k] = tile_base + ty * tiles_x + tx;
       pos[k] = bin_append(a, tile[k], tile_box(bx0, bx1, by0, by1, tx, ty, a.tile_shift));
     }
   }
@@ -509,7 +510,7 @@ __device__ __forceinline__ bool bin_record_direct(const FrameArgs& a, uint32_t r
   const uint32_t ty0 = (uint32_t)t.by0 >> a.tile_shift, ty1 = (uint32_t)t.by1 >> a.tile_shift;
   const uint32_t ntiles = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
   if (ntiles > (uint32_t)kBinDirectMax) return true;
-  bin_direct(a, vw, tx0, tx1, ty0, ty1, t.bx0, t.bx1, t.by0, t.by1, r);
+  bin_direct(a, vw.tile_base, (uint32_t)vw.tiles_x, tx0, tx1, ty0, ty1, t.bx0, t.bx1, t.by0, t.by1, r);
   return false;
 }
 
@@ -544,7 +545,7 @@ __device__ __forceinline__ void bin_tiles_warp(const FrameArgs& a, uint32_t r, i
   }
 }
 
-// The item owning this block: kind 0 face blocks (k_project), 1 normal blocks
+// The item owning this block: kind 0 face blocks (k_cull), 1 normal blocks
 // (k_light), 2 vertex blocks (k_vertex); the bases never decrease.
 __device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
   int lo = 0, hi = a.num_items - 1;
@@ -612,21 +613,24 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_project: G faces a thread in the cheap pass, full warps of survivors in
-// the heavy one; everything but the general clipper.
+// k_cull: G faces a thread, the backface and frustum tests of every face.
+// Faces for the general clipper are queued for k_clip; faces kept whole are
+// compacted over the CTA and appended to the kept list with one atomic per
+// CTA, for k_setup.  Most faces of a closed mesh face away or miss the
+// screen, so the setup runs on full warps of kept faces instead of on the
+// few survivors of each warp, and k_clip can start as soon as this pass ends.
 // ---------------------------------------------------------------------------
-// 4 CTAs per SM (64 registers a thread) with one face a thread: the face
-// pass is latency-bound, so resident warps matter more than the few registers
-// spilled; 3 (80 registers) with more faces a thread (measured: 5 us less on
-// a 3.6 M-face frame).
 template <int G>
-__global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(const FrameArgs a) {
+__global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
   griddep_wait();
   __shared__ float s_mvp[16];
-  __shared__ float s_world[16];
   __shared__ int s_item;
   __shared__ int s_vis;
   __shared__ unsigned s_out[8];
+  constexpr int kWarps = kProjectThreads / 32;
+  __shared__ uint32_t s_wn[kWarps];
+  __shared__ uint32_t s_base;
+  __shared__ uint2 s_keep[kWarps][32 * G];  // (item, face) of the warp's kept faces
 
   const int tid = threadIdx.x;
   if (tid == 0) s_item = find_item(a, 0);
@@ -634,10 +638,7 @@ __global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(con
   const int item = s_item;
   const DevItem& it = a.items[item];
   const DevView& vw = a.views[it.view];
-  if (tid < 16) {
-    s_mvp[tid] = it.mvp[tid];
-    s_world[tid] = it.world[tid];
-  }
+  if (tid < 16) s_mvp[tid] = it.mvp[tid];
   __syncthreads();
   // Frustum.BoxVisibility of the transformed bounding box (renderer.go:268-275).
   if (tid < 8) {
@@ -665,18 +666,12 @@ __global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(con
   if (vis == 0) return;  // whole block: object outside the frustum
 
   const uint32_t fl = vw.flags;
-  const int W = vw.W, H = vw.H;
   const unsigned lane = lane_id();
   const int warp = tid >> 5;
-
-  // Pass 1, every face of the warp's group: backface and frustum tests (the
-  // clip-space corners come from k_vertex: the same arithmetic, done once per
-  // vertex).  Faces for the general clipper are queued for k_clip; faces that
-  // survive whole are compacted into the warp's list, so that pass 2 runs on
-  // full warps (most faces of a closed mesh face away or miss the screen).
-  __shared__ int s_surv[kProjectThreads / 32][32 * G];
-  int* surv = s_surv[warp];
-  int nsurv = 0;
+  // The clip-space corners come from k_vertex: the same arithmetic, done
+  // once per vertex.
+  uint2* keep_list = s_keep[warp];
+  int nkeep = 0;
   const int fgroup = ((int)blockIdx.x - it.block_base) * (kProjectThreads * G) + warp * (32 * G);
 #pragma unroll
   for (int k = 0; k < G; ++k) {
@@ -720,63 +715,94 @@ __global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(con
     }
     const bool keep = draw && !general;
     const unsigned km = __ballot_sync(FULL_MASK, keep);
-    if (keep) surv[nsurv + __popc(km & ((1u << lane) - 1u))] = f;
-    nsurv += __popc(km);
+    if (keep) keep_list[nkeep + __popc(km & ((1u << lane) - 1u))] = make_uint2((uint32_t)item, (uint32_t)f);
+    nkeep += __popc(km);
   }
-  __syncwarp();
+  // The CTA's kept faces: one atomic, each warp's run at its offset.
+  if (lane == 0) s_wn[warp] = (uint32_t)nkeep;
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      const uint32_t n = s_wn[w];
+      s_wn[w] = t;
+      t += n;
+    }
+    s_base = t ? atomicAdd(&a.work->nkept, t) : 0u;
+  }
+  __syncthreads();
+  const uint32_t base = s_base + s_wn[warp];
+  for (int k = (int)lane; k < nkeep; k += 32) {
+    const uint32_t q = base + (uint32_t)k;
+    if (q < a.kept_cap) a.kept[q] = keep_list[k];
+  }
+}
 
-  // Pass 2, the surviving faces 32 at a time: attributes, screen vertices,
-  // the bin test (TPF), setup, the record and its bins.
-  for (int k0 = 0; k0 < nsurv; k0 += 32) {
-    const bool valid = k0 + (int)lane < nsurv;
-    const int f = valid ? surv[k0 + lane] : 0;
+// ---------------------------------------------------------------------------
+// k_setup: the faces k_cull kept, 32 a warp over the whole list: attributes,
+// screen vertices, the bin test (TPF), setup, the record and its bins.  A
+// warp's faces may belong to different items and views.
+// ---------------------------------------------------------------------------
+// 2 CTAs per SM (up to 128 registers a thread, no spills): measured 3 us
+// less than 4 CTAs with spills on a 200k-face frame, 24 us less on 3.6 M faces.
+__global__ void __launch_bounds__(kProjectThreads, kSetupCtasPerSm) k_setup(const FrameArgs a) {
+  griddep_wait();
+  const uint32_t nkept = min(*(volatile uint32_t*)&a.work->nkept, a.kept_cap);
+  const unsigned lane = lane_id();
+  // consecutive chunks of 32 go to different CTAs, so that the SMs share a short list evenly
+  const uint32_t gwarp = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t k0 = gwarp * 32u; k0 < nkept; k0 += warps * 32u) {
+    // the record of kept face k is record k: no atomic, no second setup
+    const uint32_t r = k0 + lane;
+    const bool valid = r < nkept;
+    const uint2 e = a.kept[valid ? r : 0u];  // (item, face)
+    const DevItem& it = a.items[e.x];
+    const int f = (int)e.y;
+    const int view = it.view;
+    const uint32_t vbase = it.vert_base, okey = (it.face_base + e.y) * (uint32_t)kKeysPerFace + 1u;
+    const DevView& vw = a.views[view];
+    const uint32_t fl = vw.flags;
+    const int W = vw.W, H = vw.H;
+    const uint32_t tile_base = vw.tile_base, tiles_x = (uint32_t)vw.tiles_x;
     bool emit = false;   // this face yields one record
     int ntpf = 0;
     int tex = -1;
     SV s0, s1, s2;
+    Setup s;
     if (valid) {
+      PV p0, p1, p2;
       const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
-      const float w0 = __ldg(&a.vclip[it.vert_base + i0].w), w1 = __ldg(&a.vclip[it.vert_base + i1].w),
-                  w2 = __ldg(&a.vclip[it.vert_base + i2].w);
-      {
-        PV p0, p1, p2;
-        face_attributes(a, it, f, i0, i1, i2, s_world, p0, p1, p2, tex);
-        s0 = sv_of(__ldg(a.vscr + it.vert_base + i0), w0, p0);
-        s1 = sv_of(__ldg(a.vscr + it.vert_base + i1), w1, p1);
-        s2 = sv_of(__ldg(a.vscr + it.vert_base + i2), w2, p2);
-        if (bin_test(s0, s1, s2, (float)W, (float)H)) {
-          ntpf = 1;
-          Setup s;
-          // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
-          emit = (fl & 0x02u) && setup_tri(s0, s1, s2, W, H, s);
-        }
+      const uint32_t v0 = vbase + i0, v1 = vbase + i1, v2 = vbase + i2;
+      face_attributes(a, it, f, i0, i1, i2, it.world, p0, p1, p2, tex);
+      s0 = sv_of(__ldg(a.vscr + v0), __ldg(&a.vclip[v0].w), p0);
+      s1 = sv_of(__ldg(a.vscr + v1), __ldg(&a.vclip[v1].w), p1);
+      s2 = sv_of(__ldg(a.vscr + v2), __ldg(&a.vclip[v2].w), p2);
+      if (bin_test(s0, s1, s2, (float)W, (float)H)) {
+        ntpf = 1;
+        // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
+        emit = (fl & 0x02u) && setup_tri(s0, s1, s2, W, H, s);
       }
     }
 
-    // TPF: one atomic per warp (all faces of a block belong to one view).
-    const int wt = __reduce_add_sync(FULL_MASK, ntpf);
-    if (lane == 0 && wt) atomicAdd(&a.view_tpf[it.view], (unsigned long long)wt);
-    if (fl & 0xC0u)  // ShowEdges / ShowVertices: every binned triangle leaves marks
-      emit_overlay(a, ntpf != 0, s0, s1, s2, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u, it.view);
-
-    // Compact records: one atomic per warp, lane offsets from the ballot.
-    const unsigned em = __ballot_sync(FULL_MASK, emit);
-    if (em == 0) continue;
-    uint32_t base = 0;
-    const int ldr = __ffs(em) - 1;
-    if ((int)lane == ldr) {
-      base = atomicAdd(&a.work->nrec, (uint32_t)__popc(em));
-      if (base + (uint32_t)__popc(em) > a.rec_cap) atomicMax(&a.work->rec_need, base + (uint32_t)__popc(em));
+    // TPF: one atomic per view present in the warp (nearly always one).
+    unsigned pend = __ballot_sync(FULL_MASK, ntpf != 0);
+    while (pend) {
+      const int ldr = __ffs(pend) - 1;
+      const int v = __shfl_sync(FULL_MASK, view, ldr);
+      const unsigned mine = __ballot_sync(FULL_MASK, ntpf != 0 && view == v);
+      if ((int)lane == ldr) atomicAdd(&a.view_tpf[v], (unsigned long long)__popc(mine));
+      pend &= ~mine;
     }
-    base = __shfl_sync(FULL_MASK, base, ldr);
-    const uint32_t r = base + __popc(em & ((1u << lane) - 1u));
+    if (__any_sync(FULL_MASK, fl & 0xC0u))  // ShowEdges / ShowVertices: every binned triangle leaves marks
+      emit_overlay(a, ntpf != 0 && (fl & 0xC0u), s0, s1, s2, okey, view);
+
     const bool ok = emit && r < a.rec_cap;
+    if (emit && !ok) atomicMax(&a.work->rec_need, r + 1u);
     uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
     int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
     if (ok) {
-      Setup s;
-      setup_tri(s0, s1, s2, W, H, s);
-      write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + 1u);
+      write_record(a, r, s, s0, s1, s2, tex, okey);
       pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
       tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
       tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
@@ -784,23 +810,38 @@ __global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(con
       ty1 = (uint32_t)s.r.by1 >> a.tile_shift;
     }
     const uint32_t ntiles = ok ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0u;
-    // single-tile triangles: warp-aggregated append per distinct tile
-    const bool one = ntiles == 1;
-    const unsigned m1 = __ballot_sync(FULL_MASK, one);
-    if (one) {
-      const uint32_t tile = vw.tile_base + ty0 * (uint32_t)vw.tiles_x + tx0;
-      const unsigned grp = __match_any_sync(m1, tile);
-      const int leader = __ffs(grp) - 1;
-      const unsigned rank = __popc(grp & ((1u << lane) - 1u));
-      uint32_t pos = 0;
-      const uint32_t box = (uint32_t)((pbx1 - pbx0 + 1) * (pby1 - pby0 + 1));
-      if (box > (uint32_t)kSmallBox) atomicAdd(&a.tile_cost[tile], box);
-      if ((int)lane == leader) pos = atomicAdd(&a.bin_count[tile], (uint32_t)__popc(grp));
-      pos = __shfl_sync(grp, pos, leader) + rank;
-      bin_store(a, tile, pos, r);
+    // One to four tiles: the k-th tile of every lane's box in round k, one
+    // bin-count atomic per distinct tile of the round (neighbouring faces
+    // share tiles, and the hot tiles of a frame take hundreds of entries:
+    // per-lane atomics on them serialise).  All rounds' atomics are issued
+    // before any result is used, so their round trips overlap.
+    const uint32_t nx = tx1 - tx0 + 1;
+    uint32_t tile[kBinDirectMax], grp[kBinDirectMax], pos[kBinDirectMax];
+#pragma unroll
+    for (int k = 0; k < kBinDirectMax; ++k) {
+      const bool act = (uint32_t)k < ntiles && ntiles <= (uint32_t)kBinDirectMax;
+      const unsigned am = __ballot_sync(FULL_MASK, act);
+      grp[k] = 0u;
+      pos[k] = 0u;
+      if (act) {
+        const uint32_t dy = (uint32_t)k / nx, tx = tx0 + ((uint32_t)k - dy * nx), ty = ty0 + dy;
+        tile[k] = tile_base + ty * tiles_x + tx;
+        grp[k] = __match_any_sync(am, tile[k]);
+        const uint32_t box = tile_box(pbx0, pbx1, pby0, pby1, tx, ty, a.tile_shift);
+        const uint32_t cost = __reduce_add_sync(grp[k], box > (uint32_t)kSmallBox ? box : 0u);
+        if ((int)lane == __ffs(grp[k]) - 1) {
+          if (cost) atomicAdd(&a.tile_cost[tile[k]], cost);
+          pos[k] = atomicAdd(&a.bin_count[tile[k]], (uint32_t)__popc(grp[k]));
+        }
+      }
     }
-    // two to four tiles: direct appends
-    if (ntiles > 1 && ntiles <= (uint32_t)kBinDirectMax) bin_direct(a, vw, tx0, tx1, ty0, ty1, pbx0, pbx1, pby0, pby1, r);
+#pragma unroll
+    for (int k = 0; k < kBinDirectMax; ++k) {
+      if (grp[k]) {
+        const uint32_t p = __shfl_sync(grp[k], pos[k], __ffs(grp[k]) - 1) + __popc(grp[k] & ((1u << lane) - 1u));
+        bin_store(a, tile[k], p, r);
+      }
+    }
     // more: the multi-tile queue, one atomic per warp
     const bool many = ntiles > (uint32_t)kBinDirectMax;
     const unsigned mm = __ballot_sync(FULL_MASK, many);
@@ -811,7 +852,7 @@ __global__ void __launch_bounds__(kProjectThreads, G == 1 ? 4 : 3) k_project(con
       qb = __shfl_sync(FULL_MASK, qb, l2);
       if (many) {
         const uint32_t q = qb + __popc(mm & ((1u << lane) - 1u));
-        if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)it.view);
+        if (q < a.big_cap) a.big[q] = make_uint2(r, (uint32_t)view);
         else atomicMax(&a.work->big_need, q + 1);
       }
     }
@@ -861,6 +902,7 @@ __device__ __forceinline__ SV shfl_sv(const SV& v, int src) {
 __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
   griddep_wait();
   const uint32_t nclip = min(*(volatile uint32_t*)&a.work->nclip, a.clip_cap);
+  const uint32_t nkept = *(volatile uint32_t*)&a.work->nkept;
   const int lane = (int)lane_id();
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nclip; q += warps) {
@@ -950,7 +992,7 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
       ntpf = 1;
       Setup s;
       if ((vw.flags & 0x02u) && setup_tri(s0, s1, s2, vw.W, vw.H, s)) {
-        const uint32_t r = atomicAdd(&a.work->nrec, 1u);
+        const uint32_t r = nkept + atomicAdd(&a.work->nrec, 1u);  // after the kept faces' records
         if (r < a.rec_cap) {
           write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
           many = bin_record_direct(a, r, s.r, it.view);
@@ -1809,7 +1851,7 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     DevWork* w = a.work;
     DevResult* r = a.result;
     r->tpf = 0;
-    r->nrec = w->nrec;
+    r->nrec = w->nkept + w->nrec;
     r->nbig = w->nbig;
     r->bin_need = w->bin_need;
     r->rec_need = w->rec_need;
@@ -1823,7 +1865,7 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     r->ovl_need = w->ovl_need;
     w->novl = 0; w->ovl_need = 0;
     w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
-    w->nclip = 0; w->clip_need = 0; w->max_bin = 0;
+    w->nclip = 0; w->clip_need = 0; w->max_bin = 0; w->nkept = 0;
     w->plan_front = 0; w->plan_back = 0; w->raster_next = 0; w->raster_exit = 0;
   }
   __syncthreads();
@@ -1990,17 +2032,19 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
     else k_vertex<1><<<a.vert_blocks, 256, 0, s>>>(a);
     ++n;
     if (light) join(0);
-    if (a.project_g == 4) launch_after(k_project<4>, a.total_blocks, kProjectThreads, s, a);
-    else if (a.project_g == 2) launch_after(k_project<2>, a.total_blocks, kProjectThreads, s, a);
-    else launch_after(k_project<1>, a.total_blocks, kProjectThreads, s, a);
+    if (a.project_g == 4) launch_after(k_cull<4>, a.total_blocks, kProjectThreads, s, a);
+    else if (a.project_g == 2) launch_after(k_cull<2>, a.total_blocks, kProjectThreads, s, a);
+    else launch_after(k_cull<1>, a.total_blocks, kProjectThreads, s, a);
     ++n;
-    if (events) cudaEventRecord((cudaEvent_t)events[1], s);
     const bool clip = a.flags_any & 0x01u;
-    if (clip) {
+    if (clip) {  // needs only k_cull's queue: runs beside k_setup and k_bin_big
       fork(1);
       k_clip<<<kClipBlocks, 128, 0, s2>>>(a);
       ++n;
     }
+    launch_after(k_setup, a.setup_blocks, kProjectThreads, s, a);
+    ++n;
+    if (events) cudaEventRecord((cudaEvent_t)events[1], s);
     if (events) k_bin_big<<<big_blocks, 256, 0, s>>>(a);  // timed stages: plain launches
     else launch_after(k_bin_big, big_blocks, 256, s, a);
     ++n;

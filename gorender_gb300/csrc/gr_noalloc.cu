@@ -57,7 +57,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
-  size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip,
+  size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip, kept,
       vlight, vclip, vscr, gkey, tile_done, work, result, end;
 };
 
@@ -81,6 +81,7 @@ constexpr Layout make_layout() {
   l.tile_cost = o; o += up256(sizeof(uint32_t) * kTiles);
   l.big = o; o += up256(sizeof(uint2) * kQueueCap);
   l.clip = o; o += up256(sizeof(uint2) * kQueueCap);
+  l.kept = o; o += up256(sizeof(uint2) * kMaxFaces);
   l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
   l.vclip = o; o += up256(sizeof(float4) * kMaxVertices);
   l.vscr = o; o += up256(sizeof(float2) * kMaxVertices);
@@ -260,6 +261,9 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.tile_cost = (uint32_t*)(base + kLayout.tile_cost);
   a.big = (uint2*)(base + kLayout.big);
   a.clip = (uint2*)(base + kLayout.clip);
+  a.kept = (uint2*)(base + kLayout.kept);
+  a.kept_cap = kMaxFaces;
+  a.setup_blocks = (int)std::min<long>(kSetupBlocks, (faces + kProjectThreads - 1) / kProjectThreads);
   a.vlight = (float*)(base + kLayout.vlight);
   a.vclip = (float4*)(base + kLayout.vclip);
   a.vscr = (float2*)(base + kLayout.vscr);
