@@ -146,6 +146,7 @@ struct gr_context {
   DevWork* work = nullptr;
   DevResult* d_result = nullptr;
   DevResult* h_result = nullptr;  // pinned
+  DevResult* h_result_dev = nullptr;  // its device address (the raster writes a synchronous frame's result there)
 
   uint32_t* fb_rgba = nullptr;
   float* fb_z = nullptr;
@@ -186,15 +187,17 @@ bool is_device_ptr(const void* p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
-// Device address of page-locked host memory (null for any other pointer):
-// the kernels write a frame's outputs there directly, with no copy after it.
-void* mapped_host_ptr(void* p) {
+// One query for an output pointer: device memory (*dev), page-locked host
+// memory (returns its device address) or neither (pageable, or null).
+void* classify_out_ptr(void* p, bool* dev) {
+  *dev = false;
   if (!p) return nullptr;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
+  *dev = at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
@@ -733,11 +736,11 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
                   uint8_t* rgba_out, float* z_out, int64_t* tpf_out) {
   if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "params is NULL");
   const size_t px = (size_t)p->width * (size_t)p->height;
-  const bool rgba_dev = is_device_ptr(rgba_out), z_dev = is_device_ptr(z_out);
   // page-locked host outputs are written by the kernels through their device
   // addresses; pageable ones are copied from the context's framebuffer
-  uint32_t* rgba_map = rgba_dev ? nullptr : (uint32_t*)mapped_host_ptr(rgba_out);
-  float* z_map = z_dev ? nullptr : (float*)mapped_host_ptr(z_out);
+  bool rgba_dev, z_dev;
+  uint32_t* rgba_map = (uint32_t*)classify_out_ptr(rgba_out, &rgba_dev);
+  float* z_map = (float*)classify_out_ptr(z_out, &z_dev);
   int32_t st;
   for (int attempt = 0; attempt < 4; ++attempt) {
     uint32_t* rgba = rgba_dev ? (uint32_t*)rgba_out : rgba_map;
@@ -752,10 +755,11 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
     v.host_out = rgba_map || z_map;
     Prepared pr;
     if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
-    if ((st = launch(c, pr.a))) return st;
     // the counters and the outputs in one go: one host wait per frame (a frame
-    // whose buffers overflowed is drawn again and its outputs copied again)
-    CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
+    // whose buffers overflowed is drawn again and its outputs copied again);
+    // the last raster CTA writes the counters into page-locked memory itself
+    pr.a.result_host = c->h_result_dev;
+    if ((st = launch(c, pr.a))) return st;
     c->d2h_bytes = (int64_t)sizeof(DevResult);
     if (rgba_out && !rgba_dev) {
       if (!rgba_map) CK(cudaMemcpyAsync(rgba_out, rgba, px * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -814,6 +818,7 @@ int32_t gr_context_create(int32_t device, gr_context** out) {
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_result, sizeof(DevResult));
   if (e == cudaSuccess) e = cudaMemset(c->d_result, 0, sizeof(DevResult));
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_result, sizeof(DevResult));
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c->h_result_dev, c->h_result, 0);
   for (int i = 0; i < 64 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->events[i]);
   for (int i = 0; i < kStageSlots && e == cudaSuccess; ++i)
     e = cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming);

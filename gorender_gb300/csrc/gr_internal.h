@@ -148,11 +148,12 @@ struct DevWork {
   unsigned int nkept;               // faces k_cull kept whole, for k_setup
 };
 
-struct DevResult {
+struct alignas(8) DevResult {
   unsigned long long tpf;           // binned triangles over all views
   unsigned int nrec, nbig, bin_need, rec_need, big_need, error, nclip, clip_need, max_bin, items;
   unsigned int novl, ovl_need;
 };
+static_assert(sizeof(DevResult) % sizeof(unsigned) == 0, "DevResult is copied word by word");
 
 // Everything a frame's kernels need, passed by value.
 struct FrameArgs {
@@ -197,6 +198,8 @@ struct FrameArgs {
   uint32_t slice_cost;              // raster cost per slice (k_plan splits costlier tiles)
   DevWork* work;
   DevResult* result;
+  DevResult* result_host;           // device address of page-locked host memory that the last raster
+                                    // CTA copies the result into (null: the host copies it)
   unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)
   unsigned long long* view_tpf_out; // per view: published by k_plan
   uint2* plan;                      // raster work items (tile, slice | view << 5), plan_cap entries

@@ -1875,6 +1875,13 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     a.view_tpf[v] = 0ull;
     if (t) atomicAdd(&a.result->tpf, t);
   }
+  if (a.result_host) {  // the finished counters straight into page-locked host memory
+    __syncthreads();
+    constexpr int kWords = (int)(sizeof(DevResult) / sizeof(unsigned));
+    if (threadIdx.x < kWords)
+      reinterpret_cast<unsigned*>(a.result_host)[threadIdx.x] =
+          __ldcg(reinterpret_cast<const unsigned*>(a.result) + threadIdx.x);
+  }
 }
 
 // ---------------------------------------------------------------------------
