@@ -85,8 +85,17 @@ struct gr_context {
   int d_texs_cap = 0;
   bool texs_dirty = true;
 
+  // The draw tables: the view table and the item table side by side in one
+  // device allocation (d_views / d_items point into it), staged in
+  // kStageSlots page-locked slots of the same layout, so that a draw uploads
+  // both with one copy.
+  unsigned char* d_tables = nullptr;
+  unsigned char* h_tables = nullptr;
+  size_t tables_off = 0;            // byte offset of the item table in a slot
+  size_t tables_stride = 0;         // bytes of one slot
+  int tab_views_cap = 0;
+  DevView* d_views = nullptr;
   DevItem* d_items = nullptr;
-  DevItem* h_items = nullptr;  // pinned staging: kStageSlots slots of items_cap items
   int items_cap = 0;
   // Pinned staging ring: back-to-back asynchronous draws write the next slot;
   // a slot is rewritten only after the copies that read it have run.
@@ -120,8 +129,6 @@ struct gr_context {
   float4* vclip = nullptr;          // per item vertex: clip position and screen x, y (k_vertex)
   float2* vscr = nullptr;
   uint64_t vert_cap = 0;
-  DevView* d_views = nullptr;       // view table (device) and its pinned staging
-  DevView* h_views = nullptr;       // kStageSlots slots of views_cap views
   unsigned long long* view_tpf = nullptr;
   unsigned long long* view_tpf_out = nullptr;
   unsigned long long* h_view_tpf = nullptr;
@@ -225,18 +232,29 @@ int32_t upload(gr_context* c, T** dst, const T* src, size_t count) {
   return GR_OK;
 }
 
-int32_t ensure_items(gr_context* c, int n) {
-  if (n <= c->items_cap) return GR_OK;
-  int cap = std::max(n, 2 * c->items_cap);
+int32_t ensure_tables(gr_context* c, int nviews, int nitems) {
+  if (nviews <= c->tab_views_cap && nitems <= c->items_cap) return GR_OK;
+  const int vcap = nviews > c->tab_views_cap ? std::max(nviews, 2 * c->tab_views_cap) : c->tab_views_cap;
+  const int icap = nitems > c->items_cap ? std::max(nitems, 2 * c->items_cap) : c->items_cap;
   CK(cudaStreamSynchronize(c->stream));
-  dev_free(c->d_items);
-  if (c->h_items) cudaFreeHost(c->h_items);
-  c->h_items = nullptr;
+  dev_free(c->d_tables);
+  if (c->h_tables) cudaFreeHost(c->h_tables);
+  c->h_tables = nullptr;
+  c->d_views = nullptr;
+  c->d_items = nullptr;
+  c->tab_views_cap = 0;
   c->items_cap = 0;
-  int32_t st = dev_alloc(&c->d_items, cap);
+  const size_t off = (sizeof(DevView) * (size_t)vcap + 15) & ~(size_t)15;
+  const size_t stride = (off + sizeof(DevItem) * (size_t)icap + 255) & ~(size_t)255;
+  int32_t st = dev_alloc(&c->d_tables, stride);
   if (st) return st;
-  CK(cudaMallocHost((void**)&c->h_items, sizeof(DevItem) * cap * kStageSlots));
-  c->items_cap = cap;
+  CK(cudaMallocHost((void**)&c->h_tables, stride * kStageSlots));
+  c->tables_off = off;
+  c->tables_stride = stride;
+  c->d_views = reinterpret_cast<DevView*>(c->d_tables);
+  c->d_items = reinterpret_cast<DevItem*>(c->d_tables + off);
+  c->tab_views_cap = vcap;
+  c->items_cap = icap;
   return GR_OK;
 }
 
@@ -371,19 +389,14 @@ struct ViewIn {
 int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
   if (nviews > c->views_cap) {
     CK(cudaStreamSynchronize(c->stream));
-    dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out);
-    if (c->h_views) cudaFreeHost(c->h_views);
+    dev_free(c->view_tpf); dev_free(c->view_tpf_out);
     if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
-    c->h_views = nullptr;
     c->h_view_tpf = nullptr;
     c->views_cap = 0;
     const int cap = std::max(nviews, 2 * c->views_cap);
     int32_t st;
-    if ((st = dev_alloc(&c->d_views, cap)) || (st = dev_alloc(&c->view_tpf, cap)) ||
-        (st = dev_alloc(&c->view_tpf_out, cap)))
-      return st;
+    if ((st = dev_alloc(&c->view_tpf, cap)) || (st = dev_alloc(&c->view_tpf_out, cap))) return st;
     CK(cudaMemsetAsync(c->view_tpf, 0, sizeof(unsigned long long) * cap, c->stream));
-    CK(cudaMallocHost((void**)&c->h_views, sizeof(DevView) * cap * kStageSlots));
     CK(cudaMallocHost((void**)&c->h_view_tpf, sizeof(unsigned long long) * cap));
     c->views_cap = cap;
   }
@@ -422,7 +435,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     total_tiles += (uint32_t)t;
     flags_any |= p->flags;
   }
-  int32_t st = ensure_items(c, std::max(n, 1));
+  int32_t st = ensure_tables(c, nviews, std::max(n, 1));
   if (st) return st;
   if ((st = upload_textures(c))) return st;
   if ((st = ensure_views(c, nviews, total_tiles))) return st;
@@ -452,8 +465,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   }
   const int slot = (c->stage_slot + 1) % kStageSlots;
   if (c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
-  DevView* hviews = c->h_views + (size_t)slot * c->views_cap;
-  DevItem* hitems = c->h_items + (size_t)slot * c->items_cap;
+  unsigned char* hslot = c->h_tables + (size_t)slot * c->tables_stride;
+  DevView* hviews = reinterpret_cast<DevView*>(hslot);
+  DevItem* hitems = reinterpret_cast<DevItem*>(hslot + c->tables_off);
   uint32_t tile_base = 0;
   uint64_t pix_base = 0;
   for (int v = 0; v < nviews; ++v) {
@@ -563,12 +577,18 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // a graph batch keeps its own tables, so other draws cannot overwrite them
   DevView* dviews = own_views ? own_views : c->d_views;
   DevItem* ditems = own_items ? own_items : c->d_items;
-  CK(cudaMemcpyAsync(dviews, hviews, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
-  if (live) CK(cudaMemcpyAsync(ditems, hitems, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+  if (!own_views && !own_items) {  // both tables with one copy
+    const size_t bytes = live ? c->tables_off + sizeof(DevItem) * (size_t)live : sizeof(DevView) * (size_t)nviews;
+    CK(cudaMemcpyAsync(c->d_tables, hslot, bytes, cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes = (int64_t)bytes;
+  } else {
+    CK(cudaMemcpyAsync(dviews, hviews, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
+    if (live) CK(cudaMemcpyAsync(ditems, hitems, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
+  }
   CK(cudaEventRecord(c->stage_ev[slot], c->stream));
   c->stage_used[slot] = true;
   c->stage_slot = slot;
-  c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
   c->d2h_bytes = 0;
 
   FrameArgs& a = out.a;
@@ -847,15 +867,14 @@ int32_t gr_context_destroy(gr_context* c) {
     dev_free(m.vidx); dev_free(m.nidx); dev_free(m.tex);
   }
   for (auto& t : c->texs) if (t.px) cudaFree(t.px);
-  dev_free(c->d_texs); dev_free(c->d_items);
-  if (c->h_items) cudaFreeHost(c->h_items);
+  dev_free(c->d_texs); dev_free(c->d_tables);
+  if (c->h_tables) cudaFreeHost(c->h_tables);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->kept); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);
-  dev_free(c->d_views); dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan); dev_free(c->empty_tiles);
+  dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan); dev_free(c->empty_tiles);
   dev_free(c->ovl); dev_free(c->ovl_key); dev_free(c->pkey);
-  if (c->h_views) cudaFreeHost(c->h_views);
   if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
   dev_free(c->work); dev_free(c->d_result);
   if (c->h_result) cudaFreeHost(c->h_result);
