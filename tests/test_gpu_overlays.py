@@ -72,13 +72,22 @@ def test_overlays_every_tile_size_twice(tile):
         ctx.close()
 
 
-def test_batched_views_with_overlays():
+# overlay flags per view k: every view marked, or only every third view (a
+# warp of kept faces then mixes faces of views with and without marks)
+OVERLAY_PATTERNS = {
+    "all": lambda k: EDGES if k % 2 else VERTS,
+    "some": lambda k: (EDGES | VERTS) if k % 3 == 1 else 0,
+}
+
+
+@pytest.mark.parametrize("pattern", sorted(OVERLAY_PATTERNS))
+def test_batched_views_with_overlays(pattern):
     torch = pytest.importorskip("torch")
     ctx = gr.Context(0)
     try:
         vs = scenes.multiview_batch(6, seed=2, min_tris=100, max_tris=5000,
                                     resolutions=((96, 64), (128, 128), (130, 77)))
-        vs = [dataclasses.replace(v, flags=v.flags | (EDGES if k % 2 else VERTS)) for k, v in enumerate(vs)]
+        vs = [dataclasses.replace(v, flags=v.flags | OVERLAY_PATTERNS[pattern](k)) for k, v in enumerate(vs)]
         views, entries, singles, bufs = [], [], [], []
         for v, sc in enumerate(vs):
             up = gr.UploadedScene(ctx, sc)
