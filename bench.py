@@ -231,7 +231,12 @@ def run_ours(args):
     h2d = C.c_int64()
     d2h = C.c_int64()
     N.check(L.gr_context_last_transfer_bytes(ctx.handle, C.byref(h2d), C.byref(d2h)))
+    # the last timed end-to-end frame, checked against the oracle outside the timed region
+    host = np.frombuffer((C.c_uint8 * (npx * 8)).from_address(hp.value), np.uint8)
+    last_rgba = host[:npx * 4].reshape(H, W, 4).copy()
+    last_z = host[npx * 4:].view(np.float32).reshape(H, W).copy()
     N.check(L.gr_host_free(hp))
+    parity = frame_parity(scene, last_rgba, last_z, int(tpf.value)) if rank == 0 else None
     e2e_value = faces * e2e_frames * ws / e2e_s / 1e6
 
     present = bench_present(ctx, up, scene, e2e_frames)
@@ -266,6 +271,8 @@ def run_ours(args):
                                 "bin_stage": "k_bin_big + the rest of k_clip (which starts beside k_setup)",
                                 "raster_stage": "k_plan + k_raster + k_resolve"},
                      "frame_algorithmic_bytes": int(ab["frame"])},
+        "parity": None if parity is None else parity["identical"],
+        "parity_check": parity,
         "gpu_launches": int(launches_per_frame * args.steps),
         "clocks": sampler.summary(),
         "e2e_present": present,
@@ -279,6 +286,20 @@ def run_ours(args):
     ctx.close()
     if pg:
         pg.destroy_process_group()
+
+
+def frame_parity(scene, rgba, z, tpf):
+    """One rendered frame against the oracle's frame of the same scene (the
+    oracle's own matrices): RGBA8 and z-buffer bit patterns and TPF."""
+    from oracle import oracle
+    oracle.build()
+    nt = max(1, min(os.cpu_count() or 1, 64))
+    ref_rgba, ref_z, ref_tpf, st = oracle.draw_scene(scene, nthreads=nt, items_override=_oracle_matrices(oracle, scene))
+    drgba = int((rgba != ref_rgba).any(axis=-1).sum())
+    dz = int((z.view(np.uint32) != ref_z.view(np.uint32)).sum())
+    return {"identical": bool(st == 0 and drgba == 0 and dz == 0 and tpf == ref_tpf), "rgba_pixels_differing": drgba,
+            "z_values_differing": dz, "tpf": tpf, "oracle_tpf": ref_tpf,
+            "rgba_sha256": __import__("hashlib").sha256(rgba.tobytes()).hexdigest()[:16]}
 
 
 def bench_batched(ctx, args, device):
@@ -347,6 +368,13 @@ def bench_batched(ctx, args, device):
                for _, bufs in plain)
     launches = ctx.last_launches()
     mb, mp = statistics.median(t_batch), statistics.median(t_plain)
+    view_tpf = b.view_tpf()
+    # every view of the last replay against the oracle's frame of that view alone
+    differing = []
+    for v, sc in enumerate(vs):
+        chk = frame_parity(sc, plain[v][1][0].cpu().numpy(), plain[v][1][1].cpu().numpy(), view_tpf[v])
+        if not chk["identical"]:
+            differing.append(v)
     b.close()
     return {"views": len(vs), "faces": faces, "pixels": pixels,
             "graph_ms": round(mb, 4), "plain_ms": round(mp, 4),
@@ -354,6 +382,7 @@ def bench_batched(ctx, args, device):
             "Mtris_per_s": round(faces / (mb * 1e-3) / 1e6, 2),
             "plain_Mtris_per_s": round(faces / (mp * 1e-3) / 1e6, 2),
             "speedup_vs_plain": round(mp / mb, 3), "identical_output": bool(same), "reps": reps,
+            "parity": not differing, "views_differing_from_oracle": differing,
             "tuning": tuning, "kernel_launches_per_batch": launches}
 
 
@@ -479,20 +508,28 @@ def bench_stress(device, args):
         ctx.sync()
         t.append(ctx.elapsed_ms(4, 5))
     ms = statistics.median(t)
+    rgba, z, tpf = up.render()
+    chk = frame_parity(sc, rgba, z, tpf)
     out = {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
+           "parity": chk["identical"], "parity_check": chk,
            "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
            "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0]}
     ctx.close()
     return out
 
 
+def _oracle_matrices(oracle, scene):
+    """Per-object (mvp, world) built by the oracle's own restatement of
+    projectObject (renderer.go:255-262): the CPU arms load nothing from the
+    library."""
+    fov = oracle.fov_radians(scene.fov_deg)
+    return [oracle.object_matrices(o, scene.camera, scene.width, scene.height, fov) for o in scene.objects]
+
+
 def _oracle_frames(scene, nthreads: int, budget_s: float, max_frames: int):
     from oracle import oracle
     oracle.build()
-    from gorender_gb300 import renderer as R
-    fov = R.fov_radians(scene.fov_deg)
-    mats = [R.object_matrices(o.scale, o.rotation, o.translation, scene.camera.position, scene.camera.direction,
-                              scene.camera.up, scene.width, scene.height, fov) for o in scene.objects]
+    mats = _oracle_matrices(oracle, scene)
     # first frame untimed (builds the ctypes structures, warms caches)
     oracle.draw_scene(scene, nthreads=nthreads, items_override=mats)
     times = []
@@ -533,10 +570,7 @@ def run_reference(args):
     nt = min(cores, 64)
     from oracle import oracle
     oracle.build()
-    from gorender_gb300 import renderer as R
-    fov = R.fov_radians(scene.fov_deg)
-    mats = [R.object_matrices(o.scale, o.rotation, o.translation, scene.camera.position, scene.camera.direction,
-                              scene.camera.up, scene.width, scene.height, fov) for o in scene.objects]
+    mats = _oracle_matrices(oracle, scene)
     for _ in range(min(args.warmup, 3)):
         oracle.draw_scene(scene, nthreads=nt, items_override=mats)
     # bounded sample: at most ~60 s of frames, at most K frames

@@ -39,7 +39,8 @@ EXPORTS = [
     "gr_batch_tuning", "gr_batch_destroy", "gr_context_set_raster", "gr_context_get_raster",
     "gr_context_autotune", "gr_diff_create", "gr_diff_forward", "gr_diff_backward", "gr_diff_buffers",
     "gr_diff_destroy", "gr_fog", "gr_context_set_fog", "gr_renderer_fog", "gr_presenter_create",
-    "gr_presenter_frame", "gr_presenter_flush", "gr_presenter_destroy",
+    "gr_presenter_frame", "gr_presenter_flush", "gr_presenter_destroy", "gr_device_alloc", "gr_device_free",
+    "gr_copy",
 ]
 
 
@@ -179,6 +180,9 @@ def lib() -> C.CDLL:
             "gr_presenter_frame": [vp, C.POINTER(Object), i32, C.POINTER(Camera), C.POINTER(vp), C.POINTER(C.c_int64)],
             "gr_presenter_flush": [vp, C.POINTER(vp), C.POINTER(C.c_int64)],
             "gr_presenter_destroy": [vp],
+            "gr_device_alloc": [vp, C.c_int64, C.POINTER(vp)],
+            "gr_device_free": [vp, vp],
+            "gr_copy": [vp, vp, vp, C.c_int64],
         }
         for name, args in sig.items():
             f = getattr(L, name)

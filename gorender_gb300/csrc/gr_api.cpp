@@ -1363,6 +1363,34 @@ int32_t gr_host_free(void* p) {
   return GR_OK;
 }
 
+int32_t gr_device_alloc(gr_context* c, int64_t bytes, void** out) {
+  if (!c || !out || bytes <= 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  CK(cudaMalloc(out, (size_t)bytes));
+  return GR_OK;
+}
+
+int32_t gr_device_free(gr_context* c, void* p) {
+  if (!c) return fail(GR_ERR_INVALID_ARGUMENT, "NULL context");
+  if (!p) return GR_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaFree(p));
+  return GR_OK;
+}
+
+int32_t gr_copy(gr_context* c, void* dst, const void* src, int64_t bytes) {
+  if (!c || (bytes > 0 && (!dst || !src)) || bytes < 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
+  if (bytes == 0) return GR_OK;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GR_OK;
+}
+
 int32_t gr_context_last_transfer_bytes(gr_context* c, int64_t* h2d, int64_t* d2h) {
   if (!c || !h2d || !d2h) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
   *h2d = c->h2d_bytes;

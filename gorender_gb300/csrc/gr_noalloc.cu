@@ -14,16 +14,22 @@
 // Limits (larger frames are rejected with GR_ERR_UNSUPPORTED): at most
 // kMaxFaces faces per frame, kMaxObjects objects, kMaxTextures textures,
 // kMaxNormals vertex normals across Gouraud-lit objects, kMaxVertices vertex
-// positions across objects, and a framebuffer of
-// at most kMaxSide x kMaxSide pixels.  Bins and record buffers cannot grow
-// here: a frame that would overflow them returns GR_ERR_BIN_OVERFLOW.
+// positions across objects with faces, and a framebuffer of at most
+// kMaxSide x kMaxSide pixels.  Bins and record buffers cannot grow here: a
+// frame that would overflow them returns GR_ERR_BIN_OVERFLOW.
 //
-// The array is shared by every call in the process: each call clears the
-// parts that must start at zero, and calls whose work overlaps on the GPU
-// (different streams, or different host threads on one device) race on it.
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current; make that first call
-// before any stream capture.
+// The caller's device-side indices (vertex, normal and face texture indices)
+// are checked on the GPU by k_noalloc_check before the frame's kernels run;
+// an index out of range returns GR_ERR_BAD_INDEX and nothing is drawn.
+//
+// The array is shared by every call in the process and keeps the previous
+// call's contents: each call clears the parts that must start at zero.  Two
+// calls whose GPU work overlapped would race on it; a per-device lock held
+// until the call's stream has drained keeps calls on one device from
+// overlapping (calls on different devices use different copies of the array
+// and do not wait on each other).  The first call on each device looks up the
+// array's device address with cudaGetSymbolAddress while that device is
+// current; make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -50,6 +56,7 @@ constexpr uint32_t kKeyCap = (uint32_t)kKeysPerFace * kMaxFaces + kKeysPerFace;
 constexpr uint32_t kBinCap = 1024;
 constexpr uint32_t kQueueCap = kMaxFaces + 1024;
 constexpr size_t kScratchBytes = 8u << 20;
+constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
@@ -58,7 +65,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
   size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip, kept,
-      vlight, vclip, vscr, gkey, tile_done, work, result, end;
+      vlight, vclip, vscr, gkey, tile_done, work, result, check, end;
 };
 
 constexpr Layout make_layout() {
@@ -89,14 +96,47 @@ constexpr Layout make_layout() {
   l.tile_done = o; o += up256(sizeof(uint32_t) * kTiles);
   l.work = o; o += up256(sizeof(DevWork));
   l.result = o; o += up256(sizeof(DevResult));
+  l.check = o; o += up256(sizeof(uint32_t));
   l.end = o;
   return l;
 }
 constexpr Layout kLayout = make_layout();
 static_assert(kLayout.end <= kScratchBytes, "scratch layout exceeds the static array");
 
-std::mutex g_mu;
-unsigned char* g_ptr[64] = {};  // device address of g_scratch per device
+std::mutex g_mu[kMaxDevices];             // one lock per device: calls on a device never overlap
+unsigned char* g_ptr[kMaxDevices] = {};   // device address of g_scratch per device
+
+// Bits of the index check's result word.
+constexpr uint32_t kBadVertex = 1u, kBadNormal = 2u, kBadTexture = 4u;
+
+// Checks every face's indices against its object's sizes: vertex indices in
+// [0, nv), normal indices in [0, nn) where the frame lights the object per
+// vertex (nn > 0), face texture indices below num_tex (negative = nil).  The
+// frame's kernels gather through these indices without bounds checks, so an
+// out-of-range one must stop the call before they run.  Faces are numbered
+// over all items (item i's faces start at items[i].face_base); one thread a
+// face, grid-stride.
+__global__ void k_noalloc_check(const DevItem* __restrict__ items, int n_items, uint32_t faces, int num_tex,
+                                int gouraud_frame, uint32_t* __restrict__ bad) {
+  uint32_t acc = 0;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < faces; g += gridDim.x * blockDim.x) {
+    int i = 0;
+    while (i + 1 < n_items && items[i + 1].face_base <= g) ++i;
+    const DevItem& it = items[i];
+    const uint32_t f = g - it.face_base;
+    if (f >= (uint32_t)it.nf) continue;
+    for (int k = 0; k < 3; ++k) {
+      const int v = it.vidx[3 * (size_t)f + k];
+      if (v < 0 || v >= it.nv) acc |= kBadVertex;
+      if (gouraud_frame && it.nn > 0) {
+        const int n = it.nidx[3 * (size_t)f + k];
+        if (n < 0 || n >= it.nn) acc |= kBadNormal;
+      }
+    }
+    if (it.tex && it.tex[f] >= num_tex) acc |= kBadTexture;
+  }
+  if (acc) atomicOr(bad, acc);
+}
 
 }  // namespace
 }  // namespace gr
@@ -110,7 +150,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   if (!p || !rgba_dev || !z_dev || num_objects < 0 || (num_objects > 0 && !objects) || num_textures < 0 ||
       (num_textures > 0 && !textures))
     return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: missing argument");
-  if (device < 0 || device >= 64) return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: bad device %d", device);
+  if (device < 0 || device >= kMaxDevices) return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: bad device %d", device);
   if (p->width <= 0 || p->height <= 0 || p->width > kMaxSide || p->height > kMaxSide)
     return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: framebuffer %dx%d exceeds the %dx%d limit", p->width,
                      p->height, kMaxSide, kMaxSide);
@@ -119,6 +159,8 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   if (num_textures > kMaxTextures)
     return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %d textures exceed the limit of %d", num_textures,
                      kMaxTextures);
+  if (p->flags & ~0x1FFu)
+    return set_error(GR_ERR_INVALID_ARGUMENT, "gr_draw_noalloc: unknown flag bits 0x%x", p->flags & ~0x1FFu);
   if (p->flags & (GR_SHOW_EDGES | GR_SHOW_VERTICES))
     return set_error(GR_ERR_UNSUPPORTED, "edge and vertex overlays are not implemented");
   const bool gouraud_frame = (p->flags & GR_LIGHTING) && !(p->flags & GR_FLAT_SHADING);
@@ -141,7 +183,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     return set_error(GR_ERR_UNSUPPORTED, "gr_draw_noalloc: %ld vertex normals exceed the limit of %d", normals,
                      kMaxNormals);
 
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(g_mu[device]);
   int prev = -1;
   cudaGetDevice(&prev);
   cudaError_t e = cudaSetDevice(device);
@@ -292,6 +334,23 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   if (e == cudaSuccess && live) e = cudaMemcpyAsync(base + kLayout.items, items, sizeof(DevItem) * live, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && num_textures)
     e = cudaMemcpyAsync(base + kLayout.texs, texs, sizeof(DevTex) * num_textures, cudaMemcpyHostToDevice, s);
+  // The caller's indices, checked on the GPU before any kernel gathers
+  // through them (one small launch and one wait; faces <= kMaxFaces).
+  uint32_t bad = 0;
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + kLayout.check, 0, sizeof(uint32_t), s);
+  if (e == cudaSuccess && live) {
+    k_noalloc_check<<<(unsigned)((faces + 255) / 256), 256, 0, s>>>(
+        (const DevItem*)(base + kLayout.items), live, (uint32_t)faces, num_textures, gouraud_frame ? 1 : 0,
+        (uint32_t*)(base + kLayout.check));
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, base + kLayout.check, sizeof(bad), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e == cudaSuccess && bad) {
+    if (prev >= 0) cudaSetDevice(prev);
+    return set_error(GR_ERR_BAD_INDEX, "gr_draw_noalloc: %s index out of range",
+                     (bad & kBadVertex) ? "a vertex" : (bad & kBadNormal) ? "a normal" : "a face texture");
+  }
   int launches = 0;
   if (e == cudaSuccess) e = (cudaError_t)launch_frame(a, kBigBlocks, s, &launches, nullptr);
   DevResult r;

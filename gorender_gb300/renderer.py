@@ -100,6 +100,41 @@ def fov_radians(deg: float) -> float:
 
 # ---- device objects ----
 
+class DeviceBuffer:
+    """Device memory owned through the C-ABI (gr_device_alloc / gr_device_free),
+    with host copies through gr_copy: outputs of batched views and the
+    differentiable parameters for hosts without a CUDA allocator of their own."""
+
+    def __init__(self, ctx: "Context", nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        self._p = C.c_void_p()
+        N.check(N.lib().gr_device_alloc(ctx.handle, self.nbytes, C.byref(self._p)))
+
+    @property
+    def ptr(self) -> int:
+        return int(self._p.value)
+
+    def upload(self, a: np.ndarray) -> "DeviceBuffer":
+        a = np.ascontiguousarray(a)
+        if a.nbytes > self.nbytes:
+            raise ValueError(f"{a.nbytes} bytes do not fit a {self.nbytes}-byte buffer")
+        N.check(N.lib().gr_copy(self.ctx.handle, self.ptr, a.ctypes.data, a.nbytes))
+        return self
+
+    def download(self, shape, dtype) -> np.ndarray:
+        out = np.empty(shape, dtype)
+        if out.nbytes > self.nbytes:
+            raise ValueError(f"{out.nbytes} bytes exceed the {self.nbytes}-byte buffer")
+        N.check(N.lib().gr_copy(self.ctx.handle, out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+    def free(self):
+        if self._p and self._p.value and self.ctx.handle:
+            N.check(N.lib().gr_device_free(self.ctx.handle, self._p))
+        self._p = C.c_void_p()
+
+
 class Context:
     """A gr_context: one device, one stream, resident meshes and textures."""
 
@@ -127,6 +162,10 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def device_buffer(self, nbytes: int) -> "DeviceBuffer":
+        """A device allocation on this context's GPU (gr_device_alloc)."""
+        return DeviceBuffer(self, nbytes)
 
     def texture(self, t: TextureData) -> int:
         out = C.c_int32()

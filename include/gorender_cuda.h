@@ -288,6 +288,15 @@ int32_t gr_draw_profiled(gr_context* ctx, const gr_draw_item* items, int32_t num
 /* Page-locked host memory for framebuffers read back every frame. */
 int32_t gr_host_alloc(int64_t bytes, void** out);
 int32_t gr_host_free(void* p);
+/* Device buffers on the context's GPU, for hosts without CUDA of their own
+ * (a Go host that keeps batch outputs or differentiable parameters on the
+ * device; no counterpart in the reference, whose framebuffers are Go slices,
+ * rasterizer.go:15-23).  gr_device_free waits for the context's stream first.
+ * gr_copy copies bytes between any two host or device pointers in the
+ * context's stream order and returns when the copy is done. */
+int32_t gr_device_alloc(gr_context* ctx, int64_t bytes, void** out);
+int32_t gr_device_free(gr_context* ctx, void* p);
+int32_t gr_copy(gr_context* ctx, void* dst, const void* src, int64_t bytes);
 
 /* ---- draw without allocating: no counterpart in the reference ----
  * For callers that must not allocate device memory themselves or let a
@@ -300,19 +309,24 @@ int32_t gr_host_free(void* p);
  * loads the library until the process exits).  It allocates nothing.
  *
  * Limits, checked up front (GR_ERR_UNSUPPORTED): <= 4096 faces per frame,
- * <= 16 objects, <= 16 textures, <= 16384 vertex normals across Gouraud-lit
- * objects, framebuffer <= 512 x 512.  A frame that overflows the fixed bins
- * or record buffers returns GR_ERR_BIN_OVERFLOW (nothing can grow here).
- * Device-side inputs are not validated: vertex/normal indices must be in
- * range and face texture handles must index `textures`.
+ * <= 16 objects, <= 16 textures, <= 32768 vertex positions across objects
+ * with faces, <= 16384 vertex normals across Gouraud-lit objects,
+ * framebuffer <= 512 x 512; unknown flag bits are GR_ERR_INVALID_ARGUMENT and
+ * the overlay flags (GR_SHOW_EDGES, GR_SHOW_VERTICES) GR_ERR_UNSUPPORTED.  A
+ * frame that overflows the fixed bins or record buffers returns
+ * GR_ERR_BIN_OVERFLOW (nothing can grow here).  The device-side vertex,
+ * normal and face texture indices are checked on the GPU before the frame
+ * runs: one out of range returns GR_ERR_BAD_INDEX and draws nothing.
  *
- * Concurrency: all calls share the static array (each call clears what must
- * start at zero); calls whose GPU work overlaps (other streams, other host
- * threads on the same device) race on it.  The call is synchronous: it waits
- * for `stream` (a cudaStream_t; NULL = default stream) before returning.  The
- * first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make it before any
- * stream capture. */
+ * Concurrency: all calls share the static array, which keeps the previous
+ * call's contents (each call clears what must start at zero).  Calls whose
+ * GPU work overlapped would race on it, so calls on one device are
+ * serialised by a lock held until the call's stream has drained; work the
+ * caller queues elsewhere never touches the array.  The call is synchronous:
+ * it waits for `stream` (a cudaStream_t; NULL = default stream) before
+ * returning.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make it before
+ * any stream capture. */
 typedef struct {
   gr_mesh_desc mesh;  /* DEVICE pointers; face_normals is required (NewMesh normals);
                          face_textures index the `textures` array, -1 = nil */

@@ -1,23 +1,32 @@
-"""Renders a named workload for a fixed number of iterations (for profilers).
+"""Renders a named workload for a fixed number of iterations, for profilers.
 
-    python -m gorender_gb300.profile --scene heightfield --frames 10 [--autotune]
+    python profile_frames.py --scene heightfield --frames 10 [--autotune]
 
 Scenes: uvsphere (960 tris, 640x360), heightfield (199,712 tris, 1280x720),
 icospheres (64 level-5/6 icospheres, 1920x1080), batch (the 256-view
 multi-view batch, one CUDA-graph replay per iteration) and diff (forward +
 backward of the differentiable icosphere workload, --views views at
 512x512).  Frames are issued with gr_draw_async on the context stream; the
-process exits non-zero on any error.
+process exits non-zero on any error.  Every device buffer comes from the
+library (gr_device_alloc), as a host without a CUDA allocator would get it.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes as C
+import os
+import sys
 import time
 
-from . import _native as N
-from . import renderer as R
-from . import scenes
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from gorender_gb300 import _native as N  # noqa: E402
+from gorender_gb300 import renderer as R  # noqa: E402
+from gorender_gb300 import scenes  # noqa: E402
 
 SCENES = {
     "uvsphere": scenes.scene_uvsphere_640x360,
@@ -47,17 +56,15 @@ def run_frames(args):
 
 
 def run_batch(args):
-    import torch
-
     vs = scenes.multiview_batch(256, seed=0)
     ctx = R.Context(args.device)
-    views, entries, keep = [], [], []
+    views, entries, bufs = [], [], []
     for v, sc in enumerate(vs):
         up = R.UploadedScene(ctx, sc)
-        rgba = torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
-        z = torch.empty((sc.height, sc.width), dtype=torch.float32, device="cuda")
-        keep += [rgba, z]
-        views.append((up.params, rgba.data_ptr(), z.data_ptr()))
+        rgba = ctx.device_buffer(sc.width * sc.height * 4)
+        z = ctx.device_buffer(sc.width * sc.height * 4)
+        bufs += [rgba, z]
+        views.append((up.params, rgba.ptr, z.ptr))
         entries += [(h, mvp, w, v) for h, (mvp, w) in zip(up.mesh_handles, up.matrices)]
     b = R.Batch(ctx, views, entries, autotune=args.autotune)
     t0 = time.perf_counter()
@@ -68,34 +75,37 @@ def run_batch(args):
     print(f"batch of {len(vs)} views: {args.frames} replays, {dt * 1e3 / args.frames:.4f} ms/replay, "
           f"tuning {b.tuning()}")
     b.close()
+    for x in bufs:
+        x.free()
     ctx.close()
 
 
 def run_diff(args):
-    import torch
-
     sc = scenes.diff_scene(views=args.views, size=512, level=6, tex_size=256, seed=0)
     ctx = R.Context(args.device)
 
-    def t(a):
-        return torch.as_tensor(a, dtype=torch.float32, device="cuda")
+    def dev(a):
+        a = np.ascontiguousarray(a, np.float32)
+        return ctx.device_buffer(a.nbytes).upload(a)
 
     mesh = ctx.mesh(sc.mesh)
     world, views = R.diff_views(sc)
     d = R.Diff(ctx, mesh, world, views, tex_size=sc.tex.shape[:2])
     npx = sum(w * h for w, h, _, _, _ in views)
-    p = [t(sc.mesh.pos), t(sc.vcol), t(sc.tex)]
-    target = torch.zeros((npx, 4), dtype=torch.float32, device="cuda")
-    g = [torch.empty((sc.mesh.nv, 4), device="cuda"), torch.empty((sc.mesh.nv, 3), device="cuda"),
-         torch.empty(sc.tex.shape, device="cuda")]
+    p = [dev(sc.mesh.pos), dev(sc.vcol), dev(sc.tex)]
+    target = dev(np.zeros((npx, 4), np.float32))
+    g = [ctx.device_buffer(sc.mesh.nv * 16), ctx.device_buffer(sc.mesh.nv * 12), ctx.device_buffer(sc.tex.nbytes)]
     t0 = time.perf_counter()
+    loss = 0.0
     for _ in range(args.frames):
-        loss = d.forward(p[0].data_ptr(), p[1].data_ptr(), p[2].data_ptr(), sc.light, target.data_ptr())
-        d.backward(*(x.data_ptr() for x in g))
+        loss = d.forward(p[0].ptr, p[1].ptr, p[2].ptr, sc.light, target.ptr)
+        d.backward(*(x.ptr for x in g))
     dt = time.perf_counter() - t0
     print(f"diff {args.views} views: {args.frames} forward+backward, {dt * 1e3 / args.frames:.4f} ms each, "
           f"loss {loss:.6e}")
     d.close()
+    for x in p + g + [target]:
+        x.free()
     ctx.close()
 
 
@@ -109,6 +119,8 @@ def main():
     ap.add_argument("--slice", type=int, default=0, help="raster cost per slice (0 keeps the default)")
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args()
+    from gorender_gb300 import build
+    build.build()
     if args.scene == "batch":
         run_batch(args)
     elif args.scene == "diff":

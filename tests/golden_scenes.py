@@ -4,6 +4,7 @@ import dataclasses
 import numpy as np
 
 from gorender_gb300 import scenes
+from tests.reference_models import REFERENCE_MODEL_SCENES
 
 
 def uvsphere():
@@ -62,3 +63,4 @@ GOLDEN_SCENES = {
     "overlays-uvsphere-320x180": overlays_uvsphere,
     "wire-heightfield97-320x180": overlays_wire_heightfield,
 }
+GOLDEN_SCENES.update(REFERENCE_MODEL_SCENES)

@@ -53,3 +53,15 @@ def test_loaded_manifest_scene(ctx, tmp_path):
     meshes, texs = loaders.load_obj(str(tmp_path / "ball.obj"))
     sc = scenes.SceneData("obj", 320, 200, [scenes.ObjectData(meshes[0])], cam, texs, scenes.DEFAULT_FLAGS)
     compare(ctx, sc)
+
+
+from tests.reference_models import REFERENCE_MODEL_SCENES  # noqa: E402
+
+
+@pytest.mark.parametrize("name", sorted(REFERENCE_MODEL_SCENES))
+def test_reference_sample_models(ctx, name):
+    """The reference's own cube (textured from its 512x512 atlas) and Suzanne,
+    drawn as its viewer draws them, bit for bit against the oracle."""
+    sc = REFERENCE_MODEL_SCENES[name]()
+    rgba, z, tpf = compare(ctx, sc)
+    assert tpf > 0 and (z > -1).sum() > 40000

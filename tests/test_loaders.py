@@ -9,7 +9,7 @@ import pytest
 from gorender_gb300 import loaders
 from tests import png_writer
 
-REF_MODELS = "/root/reference/models"
+REF_MODELS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_models")
 
 
 # ---- numbers: strconv.ParseFloat(s, 32) ----
@@ -215,7 +215,6 @@ def test_scene_unknown_mesh(objdir):
         loaders.load_scene(str(d / "bad.json"))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MODELS), reason="reference models not present")
 def test_reference_sample_models_load():
     meshes, texs = loaders.load_obj(os.path.join(REF_MODELS, "cube.obj"))
     assert len(meshes) == 1 and meshes[0].nv == 8 and meshes[0].nf == 12

@@ -135,3 +135,84 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     st = N.lib().gr_draw_noalloc(0, objs, 1, None, 0, C.byref(p2), rgba.data_ptr(), z.data_ptr(), None, None)
     assert st == N.GR_ERR_UNSUPPORTED
     assert b"4096" in N.lib().gr_last_error()
+
+
+def _call(scene, up, objs, texs, flags=None):
+    H, W = scene.height, scene.width
+    rgba = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    z = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    tpf = C.c_int64(-1)
+    params = up.params
+    if flags is not None:
+        params = gr.make_params(W, H, flags)
+    st = N.lib().gr_draw_noalloc(0, objs, len(scene.objects), texs, len(scene.textures), C.byref(params),
+                                 rgba.data_ptr(), z.data_ptr(), None, C.byref(tpf))
+    return st, rgba, z, tpf.value
+
+
+def _assert_matches(scene, up, objs, texs):
+    ref_rgba, ref_z, ref_tpf = up.render()
+    st, rgba, z, tpf = _call(scene, up, objs, texs)
+    N.check(st)
+    assert tpf == ref_tpf
+    assert np.array_equal(rgba.cpu().numpy(), ref_rgba)
+    assert np.array_equal(z.cpu().numpy().view(np.uint32), ref_z.view(np.uint32))
+
+
+def test_noalloc_rejects_bad_device_indices_and_flags():
+    """Indices in the caller's device buffers are checked on the GPU before the
+    frame's kernels gather through them: an out-of-range face texture or
+    vertex index returns GR_ERR_BAD_INDEX (no fault), unknown flag bits
+    GR_ERR_INVALID_ARGUMENT, and the next good call still matches gr_draw."""
+    scene = _small_textured_heightfield()
+    ctx = gr.Context(0)
+    try:
+        up = gr.UploadedScene(ctx, scene)
+        objs, texs, keep = _noalloc_inputs(scene, up)
+        m = scene.objects[0].mesh
+        good_tex, good_vidx = objs[0].mesh.face_textures, objs[0].mesh.vertex_indices
+        bad_tex = m.tex.copy()
+        bad_tex[m.nf // 2] = len(scene.textures)  # one past the last texture
+        t_bad = _dev(bad_tex, np.int32)
+        objs[0].mesh.face_textures = t_bad.data_ptr()
+        st, *_ = _call(scene, up, objs, texs)
+        assert st == N.GR_ERR_BAD_INDEX and b"texture" in N.lib().gr_last_error()
+        objs[0].mesh.face_textures = good_tex
+        bad_v = m.vidx.copy()
+        bad_v.reshape(-1)[7] = m.nv
+        v_bad = _dev(bad_v, np.int32)
+        objs[0].mesh.vertex_indices = v_bad.data_ptr()
+        st, *_ = _call(scene, up, objs, texs)
+        assert st == N.GR_ERR_BAD_INDEX and b"vertex" in N.lib().gr_last_error()
+        objs[0].mesh.vertex_indices = good_vidx
+        st, *_ = _call(scene, up, objs, texs, flags=scene.flags | 0x80000000)
+        assert st == N.GR_ERR_INVALID_ARGUMENT and b"flag" in N.lib().gr_last_error()
+        _assert_matches(scene, up, objs, texs)
+        del keep, t_bad, v_bad
+    finally:
+        ctx.close()
+
+
+def test_noalloc_bin_overflow_then_next_call_matches():
+    """A frame within the size limits whose triangles all fall into one raster
+    tile overflows the fixed 1024-entry bins: GR_ERR_BIN_OVERFLOW.  The static
+    array keeps what that frame left behind; the next call must still give
+    gr_draw's bytes."""
+    m = scenes.heightfield(46, extent=1.5, seed=3)  # 4050 faces, drawn a few pixels wide
+    cam = scenes.CameraData((0.0, 0.35, 1.2), (0.0, -0.4, -1.0), (0.0, 1.0, 0.0))
+    tiny = scenes.SceneData("hf46-one-tile", 256, 256, [scenes.ObjectData(m, scale=(0.01, 0.01, 0.01))], cam, [],
+                            scenes.DEFAULT_FLAGS | scenes.FLAT_SHADING)
+    ctx = gr.Context(0)
+    try:
+        up = gr.UploadedScene(ctx, tiny)
+        objs, texs, keep = _noalloc_inputs(tiny, up)
+        st, *_ = _call(tiny, up, objs, texs)
+        assert st == N.GR_ERR_BIN_OVERFLOW, N.lib().gr_last_error()
+        scene = _small_textured_heightfield()
+        up2 = gr.UploadedScene(ctx, scene)
+        objs2, texs2, keep2 = _noalloc_inputs(scene, up2)
+        for _ in range(2):
+            _assert_matches(scene, up2, objs2, texs2)
+        del keep, keep2
+    finally:
+        ctx.close()
