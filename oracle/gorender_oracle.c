@@ -125,9 +125,143 @@ static void mat_identity(float* m) {
   m[0] = m[5] = m[10] = m[15] = 1.0f;
 }
 
-static inline float sin32(float x) { return (float)sin((double)x); }  /* math32.go:15-17 */
-static inline float cos32(float x) { return (float)cos((double)x); }  /* math32.go:19-21 */
-static inline float tan32(float x) { return (float)tan((double)x); }  /* math32.go:23-25 */
+/* ---- Go's math.Sin / math.Cos / math.Tan (math32.go:15-25 call them on
+ * float64(x)).  On amd64 these are pure Go (no assembly), compiled without FMA
+ * fusion: the Cephes library's sin.c / tan.c algorithm (S. L. Moshier) as Go's
+ * math package restates it.  Argument reduction by pi/4: below 2^29 the
+ * Cody-Waite three-part split of pi/4, above it the Payne-Hanek reduction
+ * (K. C. Ng, "Argument reduction for huge arguments: good to the last bit",
+ * 1992) with 64-bit words of 4/pi; then the Cephes minimax polynomials on
+ * [-pi/4, pi/4] (sin: degree 13 odd, cos: degree 14 even, tan: a 3/4
+ * rational in z^2).  glibc's sin/cos/tan are a different algorithm and differ
+ * from Go's in the last bit of the double for about a quarter of arguments,
+ * which can survive the float32 rounding.  Evaluated in the order Go writes
+ * the expressions; this file is built with -ffp-contract=off. */
+static const double GO_PI4A = 7.85398125648498535156e-1;  /* pi/4 = A + B + C */
+static const double GO_PI4B = 3.77489470793079817668e-8;
+static const double GO_PI4C = 2.69515142907905952645e-15;
+static const double GO_4_OVER_PI = 0x1.45f306dc9c883p+0;  /* 4/pi correctly rounded */
+static const double GO_PI4 = 0x1.921fb54442d18p-1;        /* pi/4 correctly rounded */
+static const double GO_REDUCE_THRESHOLD = 536870912.0;    /* 2^29 */
+static const double GO_SIN[6] = {1.58962301576546568060e-10, -2.50507477628578072866e-8,
+                                 2.75573136213857245213e-6,  -1.98412698295895385996e-4,
+                                 8.33333333332211858878e-3,  -1.66666666666666307295e-1};
+static const double GO_COS[6] = {-1.13585365213876817300e-11, 2.08757008419747316778e-9,
+                                 -2.75573141792967388112e-7,  2.48015872888517045348e-5,
+                                 -1.38888888888730564116e-3,  4.16666666666665929218e-2};
+static const double GO_TANP[3] = {-1.30936939181383777646e4, 1.15351664838587416140e6,
+                                  -1.79565251976484877988e7};
+static const double GO_TANQ[5] = {1.0, 1.36812963470692954678e4, -1.32089234440210967447e6,
+                                  2.50083801823357915839e7, -5.38695755929454629881e7};
+/* 4/pi = sum_i W[i] * 2^(-64 i): its binary digits, computed from pi to 700
+ * digits.  Eight words cover every float64 converted from a float32
+ * (exponent <= 127); math32.go only ever passes those. */
+static const uint64_t GO_4PI_BITS[8] = {
+    0x0000000000000001ull, 0x45f306dc9c882a53ull, 0xf84eafa3ea69bb81ull, 0xb6c52b3278872083ull,
+    0xfca2c757bd778ac3ull, 0x6e48dc74849ba5c0ull, 0x0c925dd413a32439ull, 0xfc3bd63962534e7dull};
+
+static inline uint64_t dbits(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
+static inline double dfrom(uint64_t u) { double x; memcpy(&x, &u, 8); return x; }
+static inline uint64_t shl64(uint64_t v, unsigned n) { return n >= 64 ? 0 : v << n; }
+static inline uint64_t shr64(uint64_t v, unsigned n) { return n >= 64 ? 0 : v >> n; }
+
+/* Payne-Hanek: x >= 2^29 -> octant j (0..7, zeros mapped to the origin) and
+ * the reduced argument z in [-pi/4, pi/4]. */
+static void go_trig_reduce(double x, uint64_t* j_out, double* z_out) {
+  if (x < GO_PI4) { *j_out = 0; *z_out = x; return; }
+  uint64_t ix = dbits(x);
+  const int exp = (int)((ix >> 52) & 0x7FF) - 1023 - 52;  /* x = mantissa * 2^exp */
+  ix &= ~(0x7FFull << 52);
+  ix |= 1ull << 52;
+  const unsigned digit = (unsigned)(exp + 61) / 64, bitshift = (unsigned)(exp + 61) % 64;
+  const uint64_t z0 = shl64(GO_4PI_BITS[digit], bitshift) | shr64(GO_4PI_BITS[digit + 1], 64 - bitshift);
+  const uint64_t z1 = shl64(GO_4PI_BITS[digit + 1], bitshift) | shr64(GO_4PI_BITS[digit + 2], 64 - bitshift);
+  const uint64_t z2 = shl64(GO_4PI_BITS[digit + 2], bitshift) | shr64(GO_4PI_BITS[digit + 3], 64 - bitshift);
+  const unsigned __int128 p2 = (unsigned __int128)z2 * ix, p1 = (unsigned __int128)z1 * ix;
+  const uint64_t z2hi = (uint64_t)(p2 >> 64), z1hi = (uint64_t)(p1 >> 64), z1lo = (uint64_t)p1;
+  const uint64_t z0lo = z0 * ix;
+  const uint64_t lo = z1lo + z2hi;
+  const uint64_t carry = lo < z1lo;
+  uint64_t hi = z0lo + z1hi + carry;
+  uint64_t j = hi >> 61;
+  hi = hi << 3 | lo >> 61;
+  const unsigned lz = hi ? (unsigned)__builtin_clzll(hi) : 64;
+  const uint64_t e = (uint64_t)(1023 - (lz + 1));
+  hi = shl64(hi, lz + 1) | shr64(lo, 64 - (lz + 1));
+  hi >>= 64 - 52;
+  hi |= e << 52;
+  double z = dfrom(hi);
+  if (j & 1) { j++; j &= 7; z = z - 1.0; }
+  *j_out = j;
+  *z_out = z * GO_PI4;
+}
+
+/* x >= 0 below 2^29: octant (odd ones rounded up) and the reduced argument. */
+static void go_reduce(double x, uint64_t* j_out, double* z_out) {
+  if (x >= GO_REDUCE_THRESHOLD) { go_trig_reduce(x, j_out, z_out); return; }
+  uint64_t j = (uint64_t)(x * GO_4_OVER_PI);
+  double y = (double)j;
+  if (j & 1) { j++; y++; }
+  *j_out = j;
+  *z_out = ((x - y * GO_PI4A) - y * GO_PI4B) - y * GO_PI4C;
+}
+
+static inline double go_sin_poly(double z, double zz) {
+  return z + z * zz * ((((((GO_SIN[0] * zz) + GO_SIN[1]) * zz + GO_SIN[2]) * zz + GO_SIN[3]) * zz + GO_SIN[4]) * zz + GO_SIN[5]);
+}
+static inline double go_cos_poly(double zz) {
+  return 1.0 - 0.5 * zz + zz * zz * ((((((GO_COS[0] * zz) + GO_COS[1]) * zz + GO_COS[2]) * zz + GO_COS[3]) * zz + GO_COS[4]) * zz + GO_COS[5]);
+}
+
+double orc_go_sin(double x) {
+  if (x == 0 || isnan(x)) return x;
+  if (isinf(x)) return NAN;
+  int sign = 0;
+  if (x < 0) { x = -x; sign = 1; }
+  uint64_t j; double z;
+  go_reduce(x, &j, &z);
+  j &= 7;
+  if (j > 3) { sign = !sign; j -= 4; }
+  const double zz = z * z;
+  const double y = (j == 1 || j == 2) ? go_cos_poly(zz) : go_sin_poly(z, zz);
+  return sign ? -y : y;
+}
+
+double orc_go_cos(double x) {
+  if (isnan(x) || isinf(x)) return NAN;
+  int sign = 0;
+  x = fabs(x);
+  uint64_t j; double z;
+  go_reduce(x, &j, &z);
+  j &= 7;
+  if (j > 3) { j -= 4; sign = !sign; }
+  if (j > 1) sign = !sign;
+  const double zz = z * z;
+  const double y = (j == 1 || j == 2) ? go_sin_poly(z, zz) : go_cos_poly(zz);
+  return sign ? -y : y;
+}
+
+double orc_go_tan(double x) {
+  if (x == 0 || isnan(x)) return x;
+  if (isinf(x)) return NAN;
+  int sign = 0;
+  if (x < 0) { x = -x; sign = 1; }
+  uint64_t j; double z;
+  go_reduce(x, &j, &z);
+  const double zz = z * z;
+  double y;
+  if (zz > 1e-14)
+    y = z + z * (zz * (((GO_TANP[0] * zz) + GO_TANP[1]) * zz + GO_TANP[2]) /
+                 ((((zz + GO_TANQ[1]) * zz + GO_TANQ[2]) * zz + GO_TANQ[3]) * zz + GO_TANQ[4]));
+  else
+    y = z;
+  if (j & 2) y = -1 / y;
+  return sign ? -y : y;
+}
+
+static inline float sin32(float x) { return (float)orc_go_sin((double)x); }  /* math32.go:15-17 */
+static inline float cos32(float x) { return (float)orc_go_cos((double)x); }  /* math32.go:19-21 */
+static inline float tan32(float x) { return (float)orc_go_tan((double)x); }  /* math32.go:23-25 */
 
 static void rot_x(float a, float* m) {      /* matrix.go:32-44 */
   mat_identity(m);

@@ -201,6 +201,10 @@ void orc_perspective_matrix(float fov, float aspect, float znear, float zfar,
 void orc_screen_matrix(int32_t width, int32_t height, float* out);
 void orc_matrix_multiply(const float* a, const float* b, float* out);
 void orc_normalize3(const float* v, float* out);
+/* Go's math.Sin / Cos / Tan on float64 (math32.go:15-25 round them to float32). */
+double orc_go_sin(double x);
+double orc_go_cos(double x);
+double orc_go_tan(double x);
 
 #ifdef __cplusplus
 }

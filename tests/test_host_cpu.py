@@ -80,6 +80,24 @@ def test_object_matrices_match_oracle():
         assert np.array_equal(world.view(np.uint32), world2.view(np.uint32))
 
 
+def test_object_matrices_match_oracle_large_and_demo_angles():
+    """Rotation angles beyond 2^29 (Go's Payne-Hanek reduction), negative ones
+    and the demo mode's accumulated turns: the library's restatement of Go's
+    sin/cos/tan gives the oracle's matrices bit for bit."""
+    rng = np.random.default_rng(17)
+    big = [float(np.float32(s * 2.0 ** e)) for s, e in zip(rng.choice([-1, 1], 60), rng.uniform(20, 120, 60))]
+    demo = [float(np.float32(k * 0.01)) for k in range(0, 700, 23)]
+    for a in big + demo:
+        r = np.array([a, -a * 0.5, a * 0.25], np.float32)
+        fov = oracle.fov_radians(45.0)
+        mvp, world = gr.object_matrices((1, 1, 1), r, (0, 0, 0), (0, 0, 5), (0, 0, -1), (0, 1, 0), 800, 600, fov)
+        obj = scenes.ObjectData(None, (1.0, 1.0, 1.0), tuple(r), (0.0, 0.0, 0.0))
+        cam = scenes.CameraData((0.0, 0.0, 5.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0))
+        mvp2, world2 = oracle.object_matrices(obj, cam, 800, 600, fov)
+        assert np.array_equal(mvp.view(np.uint32), mvp2.view(np.uint32)), a
+        assert np.array_equal(world.view(np.uint32), world2.view(np.uint32)), a
+
+
 def test_screen_matrix_light_fov_match_oracle():
     for w, h in [(640, 360), (1280, 720), (1920, 1080), (643, 357)]:
         assert np.array_equal(gr.screen_matrix(w, h), oracle.screen_matrix(w, h))
