@@ -19,7 +19,14 @@ cpu_baseline the CPU restatement of the reference frame path (the oracle),
 
 --impl reference runs that CPU frame path (all host threads) as the
 reference arm, since the Go reference has no toolchain here.
-N > 1 (torchrun) renders independent replicas of the frame, one per GPU.
+N > 1 (under torchrun, or --gpus N alone, which starts one process per GPU
+itself): the frame is rendered as independent replicas, one per GPU, and
+value counts every rank's frames over the slowest rank's time; the 256-view
+batch is partitioned by view across the ranks (gorender_gb300.shard).  The
+ranks share only a gloo barrier and max-reductions of their timings.  The
+stress frame and the differentiable pass are reported at N = 1 only.
+parity      the last timed end-to-end frame (and every batch view, and the
+            stress frame) compared with the oracle outside the timed regions.
 """
 from __future__ import annotations
 
@@ -124,6 +131,30 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def config_of(scene, ws):
+    """The workload both arms report (the GPU tuning goes under "run")."""
+    return {"workload": WORKLOAD, "faces": scene.num_triangles, "width": scene.width, "height": scene.height,
+            "parallelism": f"replicas x{ws}"}
+
+
+def spawn_ranks(n):
+    """--gpus N outside a launcher: one process per GPU (RANK, LOCAL_RANK,
+    WORLD_SIZE and a rendezvous on 127.0.0.1 in each one's environment), the
+    same layout torchrun gives; rank 0 prints the line.  Returns the largest
+    exit status."""
+    import socket
+    sock = socket.socket()
+    sock.bind(("127.0.0.1", 0))
+    port = sock.getsockname()[1]
+    sock.close()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + sys.argv[1:], env=env))
+    return max(p.wait() for p in procs)
 
 
 def run_ours(args):
@@ -240,9 +271,10 @@ def run_ours(args):
     e2e_value = faces * e2e_frames * ws / e2e_s / 1e6
 
     present = bench_present(ctx, up, scene, e2e_frames)
-    batched = bench_batched(ctx, args, local) if not args.skip_batched else None
-    stress = bench_stress(local, args) if not args.skip_batched else None
-    diff = bench_diff(local) if not args.skip_batched else None
+    batched = bench_batched(ctx, args, local, pg) if not args.skip_batched else None
+    # the stress frame and the differentiable pass are single-GPU lines
+    stress = bench_stress(local, args) if not args.skip_batched and ws == 1 else None
+    diff = bench_diff(local) if not args.skip_batched and ws == 1 else None
 
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -255,10 +287,10 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64",
         "data": "synthetic (seeded heightfield, seeded 16x16 RGBA8 texture)",
-        "config": {"workload": WORKLOAD, "faces": faces, "width": W, "height": H,
-                   "binned_triangles": int(tpf.value), "parallelism": f"replicas x{ws}",
-                   "l2": "flushed between frames (512 MiB write outside the timed events)",
-                   "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_cost": tuning[2]},
+        "config": config_of(scene, ws),
+        "run": {"binned_triangles": int(tpf.value),
+                "l2": "flushed between frames (512 MiB write outside the timed events)",
+                "tile_size": tuning[0], "bin_capacity": tuning[1], "slice_cost": tuning[2]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
                 "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
@@ -302,51 +334,47 @@ def frame_parity(scene, rgba, z, tpf):
             "rgba_sha256": __import__("hashlib").sha256(rgba.tobytes()).hexdigest()[:16]}
 
 
-def bench_batched(ctx, args, device):
+def bench_batched(ctx, args, device, pg=None):
     """256 seeded views (heightfields and icospheres, 100..200k triangles
     log-uniform, four resolutions, mixed materials): one autotuned CUDA-graph
     batch against the same views drawn by plain per-view launches
     (gr_draw_async, one per view, back to back on the same stream).  Both are
-    device-timed with events on the library stream; outputs (820 MB) exceed
-    L2, so no flush is needed.  The two outputs are compared bit for bit."""
-    import torch
-    from gorender_gb300 import renderer as R
-    from gorender_gb300 import scenes
+    device-timed with events on the library stream; outputs (820 MB over all
+    views) exceed L2, so no flush is needed.  Each rank renders the views the
+    partition by view gives it (all of them at N = 1); the timed durations
+    are the maximum over ranks.  The batch's frames are compared with the
+    plain launches' bit for bit and every view with the oracle's frame of
+    that view alone (outside the timed regions)."""
+    import hashlib
 
+    from gorender_gb300 import renderer as R
+    from gorender_gb300 import scenes, shard
+
+    ws, rank, _ = shard.dist_env()
     vs = scenes.multiview_batch(256, seed=0)
-    dev = torch.device("cuda", device)
-    views, entries, plain = [], [], []
-    for v, sc in enumerate(vs):
-        up = R.UploadedScene(ctx, sc)
-        bufs = [torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device=dev),
-                torch.empty((sc.height, sc.width), dtype=torch.float32, device=dev),
-                torch.empty((sc.height, sc.width, 4), dtype=torch.uint8, device=dev),
-                torch.empty((sc.height, sc.width), dtype=torch.float32, device=dev)]
-        views.append((up.params, bufs[0].data_ptr(), bufs[1].data_ptr()))
-        for h, (mvp, w) in zip(up.mesh_handles, up.matrices):
-            entries.append((h, mvp, w, v))
-        plain.append((up, bufs))
-    torch.cuda.synchronize(dev)
-    faces = sum(sc.num_triangles for sc in vs)
-    pixels = sum(sc.width * sc.height for sc in vs)
-    b = R.Batch(ctx, views, entries, autotune=True)
-    tuning = b.tuning()
+    mine = shard.shard_of(vs, rank, ws)
+    sb = shard.ShardedBatch(ctx, vs, mine, autotune=True)
+    plain_out = [(ctx.device_buffer(sc.width * sc.height * 4), ctx.device_buffer(sc.width * sc.height * 4))
+                 for sc in sb.scenes]
+    tuning = sb.batch.tuning()
     reps = 10
     for _ in range(3):
-        b.run()
-    b.sync()
+        sb.run()
+    sb.sync()
     ctx.sync()
+    if pg:
+        pg.barrier()
     t_batch = []
     for _ in range(reps):
         ctx.event(0)
-        b.run()
+        sb.run()
         ctx.event(1)
-        b.sync()
+        sb.sync()
         t_batch.append(ctx.elapsed_ms(0, 1))
 
     def plain_pass():
-        for up, bufs in plain:
-            R.draw_async(ctx, up.items, len(up.scene.objects), up.params, bufs[2].data_ptr(), bufs[3].data_ptr())
+        for up, (r, z) in zip(sb.uploads, plain_out):
+            R.draw_async(ctx, up.items, len(up.scene.objects), up.params, r.ptr, z.ptr)
 
     for _ in range(2):
         plain_pass()
@@ -355,6 +383,8 @@ def bench_batched(ctx, args, device):
         except R.N.GrError as e:  # the first pass may grow the bins; it is re-issued
             if e.code != R.N.GR_ERR_BIN_OVERFLOW:
                 raise
+    if pg:
+        pg.barrier()
     t_plain = []
     for _ in range(reps):
         ctx.event(2)
@@ -362,21 +392,36 @@ def bench_batched(ctx, args, device):
         ctx.event(3)
         ctx.sync()
         t_plain.append(ctx.elapsed_ms(2, 3))
-    b.run()
-    b.sync()
-    same = all(torch.equal(bufs[0], bufs[2]) and torch.equal(bufs[1].view(torch.int32), bufs[3].view(torch.int32))
-               for _, bufs in plain)
+    sb.run()
+    sb.sync()
     launches = ctx.last_launches()
+    view_tpf = sb.view_tpf()
     mb, mp = statistics.median(t_batch), statistics.median(t_plain)
-    view_tpf = b.view_tpf()
-    # every view of the last replay against the oracle's frame of that view alone
-    differing = []
-    for v, sc in enumerate(vs):
-        chk = frame_parity(sc, plain[v][1][0].cpu().numpy(), plain[v][1][1].cpu().numpy(), view_tpf[v])
-        if not chk["identical"]:
-            differing.append(v)
-    b.close()
-    return {"views": len(vs), "faces": faces, "pixels": pixels,
+    same, differing = True, []
+    for k, sc in enumerate(sb.scenes):
+        rgba, z = sb.frame(k)
+        pr = plain_out[k][0].download(rgba.shape, np.uint8)
+        pz = plain_out[k][1].download(z.shape, np.float32)
+        same = same and np.array_equal(rgba, pr) and np.array_equal(z.view(np.uint32), pz.view(np.uint32))
+        if not frame_parity(sc, rgba, z, view_tpf[k])["identical"]:
+            differing.append(mine[k])
+    my_faces = sb.faces
+    for r, z in plain_out:
+        r.free()
+        z.free()
+    sb.close()
+    if pg:
+        import torch
+        t = torch.tensor([mb, mp, 0.0 if same else 1.0, float(len(differing))], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        mb, mp = float(t[0]), float(t[1])
+        same = same and float(t[2]) == 0.0
+        if float(t[3]) > 0 and not differing:
+            differing = ["on another rank"]
+    faces = sum(sc.num_triangles for sc in vs)
+    pixels = sum(sc.width * sc.height for sc in vs)
+    return {"views": len(vs), "faces": faces, "pixels": pixels, "ranks": ws, "views_this_rank": len(mine),
+            "faces_this_rank": my_faces, "partition": "by view, cost = faces + pixels/4, largest first",
             "graph_ms": round(mb, 4), "plain_ms": round(mp, 4),
             "views_per_s": round(len(vs) / (mb * 1e-3), 1), "plain_views_per_s": round(len(vs) / (mp * 1e-3), 1),
             "Mtris_per_s": round(faces / (mb * 1e-3) / 1e6, 2),
@@ -393,17 +438,16 @@ def bench_diff(device):
     rendered from parameters perturbed by N(0, 0.05).  Each call is timed with
     events on the library stream (the calls return after their results are on
     the host: the loss, the light gradient)."""
-    import torch
     import gorender_gb300 as gr
     from gorender_gb300 import renderer as R
     from gorender_gb300 import scenes
 
     sc = scenes.diff_scene(views=64, size=512, level=6, tex_size=256, seed=0)
     ctx = gr.Context(device)
-    dev = torch.device("cuda", device)
 
     def t(a):
-        return torch.as_tensor(a, dtype=torch.float32, device=dev)
+        a = np.ascontiguousarray(a, np.float32)
+        return ctx.device_buffer(a.nbytes).upload(a)
 
     mesh = ctx.mesh(sc.mesh)
     world, views = R.diff_views(sc)
@@ -412,18 +456,17 @@ def bench_diff(device):
     p = [t(sc.mesh.pos), t(sc.vcol), t(sc.tex)]
     tp = sc.target_params
     q = [t(tp["pos"]), t(tp["vcol"]), t(tp["tex"])]
-    target = torch.zeros((npx, 4), dtype=torch.float32, device=dev)
-    zeros = torch.zeros_like(target)
-    d.forward(q[0].data_ptr(), q[1].data_ptr(), q[2].data_ptr(), tp["light"], zeros.data_ptr(), target.data_ptr())
-    g = [torch.empty((sc.mesh.nv, 4), device=dev), torch.empty((sc.mesh.nv, 3), device=dev),
-         torch.empty(sc.tex.shape, device=dev)]
-    torch.cuda.synchronize(dev)
+    target = t(np.zeros((npx, 4), np.float32))
+    zeros = t(np.zeros((npx, 4), np.float32))
+    d.forward(q[0].ptr, q[1].ptr, q[2].ptr, tp["light"], zeros.ptr, target.ptr)
+    g = [ctx.device_buffer(sc.mesh.nv * 16), ctx.device_buffer(sc.mesh.nv * 12), ctx.device_buffer(sc.tex.nbytes)]
+    ctx.sync()
 
     def fwd():
-        return d.forward(p[0].data_ptr(), p[1].data_ptr(), p[2].data_ptr(), sc.light, target.data_ptr())
+        return d.forward(p[0].ptr, p[1].ptr, p[2].ptr, sc.light, target.ptr)
 
     def bwd():
-        return d.backward(*(x.data_ptr() for x in g))
+        return d.backward(*(x.ptr for x in g))
 
     for _ in range(3):
         fwd()
@@ -441,6 +484,8 @@ def bench_diff(device):
         tb.append(ctx.elapsed_ms(7, 8))
     mf, mb = statistics.median(tf), statistics.median(tb)
     d.close()
+    for x in p + q + g + [target, zeros]:
+        x.free()
     ctx.close()
     return {"workload": "diff-icosphere6-81920f-64views-512x512-tex256", "views": 64, "faces": sc.mesh.nf,
             "pixels": npx, "forward_ms": round(mf, 4), "backward_ms": round(mb, 4),
@@ -571,7 +616,7 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     mats = _oracle_matrices(oracle, scene)
-    for _ in range(min(args.warmup, 3)):
+    for _ in range(args.warmup):
         oracle.draw_scene(scene, nthreads=nt, items_override=mats)
     # bounded sample: at most ~60 s of frames, at most K frames
     t0 = time.perf_counter()
@@ -584,11 +629,10 @@ def run_reference(args):
     value = scene.num_triangles * frames / el / 1e6
     out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mtris/s", "n_gpus": ws,
-        "steps": frames, "warmup": min(args.warmup, 3), "ms_per_step": round(el * 1e3 / frames, 3),
+        "steps": frames, "warmup": args.warmup, "ms_per_step": round(el * 1e3 / frames, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64",
         "data": "synthetic (seeded heightfield, seeded 16x16 RGBA8 texture)",
-        "config": {"workload": WORKLOAD, "faces": scene.num_triangles, "width": scene.width,
-                   "height": scene.height, "parallelism": "cpu"},
+        "config": config_of(scene, ws),
         "cpu_baseline": {"value": round(value, 4), "unit": "Mtris/s", "cores": nt, "kind": "port",
                          "sample": f"{frames} of the requested {args.steps} frames (bounded at 60 s) "
                                    f"on {nt} threads: C restatement of the reference frame path"},
@@ -607,6 +651,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args.gpus))
     if args.impl == "reference":
         run_reference(args)
     else:

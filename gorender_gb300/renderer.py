@@ -200,7 +200,12 @@ class Context:
         tex = m.tex
         if tex is not None and texture_map is not None:
             tm = np.asarray(texture_map, np.int32)
-            tex = np.where(tex >= 0, tm[np.clip(tex, 0, len(tm) - 1)], -1).astype(np.int32)
+            if len(tm) == 0:
+                if (tex >= 0).any():
+                    raise ValueError("faces name textures but the scene has none")
+                tex = np.full(tex.shape, -1, np.int32)
+            else:
+                tex = np.where(tex >= 0, tm[np.clip(tex, 0, len(tm) - 1)], -1).astype(np.int32)
         d.face_textures = _ptr(arr(tex, np.int32))
         d.face_normals = None
         d.vertex_colors = _ptr(arr(m.vcolor, np.float32))

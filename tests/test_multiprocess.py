@@ -1,19 +1,29 @@
-"""Two-rank gloo run of the multi-GPU layout on CPU.
+"""Multi-GPU layout, run as two gloo ranks.
 
-The frame path does not shard: N GPUs render N independent replicas and the
+A single frame does not shard: N GPUs render N independent replicas and the
 only collectives are a barrier and a max over ranks of the timed duration.
-This runs that protocol with two CPU ranks, each rendering the frame with the
-oracle, and checks that the replicas agree and the reduction is a max."""
+A batch of views shards by view (gorender_gb300.shard): each rank renders the
+views the partition gives it.  These tests run both protocols with two ranks
+and check that the replicas agree, that the reduction is a max, and that the
+union of the ranks' per-view frames is exactly the single-rank set.  Without
+a GPU the ranks render with the oracle; the GPU variant renders each rank's
+share with the library's CUDA-graph batch (both ranks on GPU 0, independent
+processes whose kernels never wait on each other)."""
 import hashlib
 import os
 import socket
+import sys
 
 import numpy as np
 import pytest
 
+from gorender_gb300 import scenes, shard
+
 torch = pytest.importorskip("torch")
 import torch.distributed as dist  # noqa: E402
 import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _free_port():
@@ -24,32 +34,115 @@ def _free_port():
     return p
 
 
-def _rank(rank, world, port, q):
-    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+def _init(rank, world, port):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    import sys
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, ROOT)
+
+
+def _digest(rgba, z):
+    return hashlib.sha256(np.ascontiguousarray(rgba).tobytes() + np.ascontiguousarray(z).tobytes()).hexdigest()
+
+
+def _views():
+    return scenes.multiview_batch(18, seed=21, min_tris=100, max_tris=20000,
+                                  resolutions=((96, 64), (128, 128), (160, 90), (200, 120)))
+
+
+def _replica_rank(rank, world, port, q):
+    _init(rank, world, port)
     from oracle import oracle
     from tests.golden_scenes import heightfield_small
     dist.barrier()
     rgba, z, tpf, st = oracle.draw_scene(heightfield_small(), nthreads=1)
     elapsed = torch.tensor([float(rank + 1)], dtype=torch.float64)  # stand-in durations 1, 2
     dist.all_reduce(elapsed, op=dist.ReduceOp.MAX)
-    h = hashlib.sha256(rgba.tobytes() + z.tobytes()).hexdigest()
-    q.put((rank, st, tpf, h, float(elapsed.item())))
+    q.put((rank, st, tpf, _digest(rgba, z), float(elapsed.item())))
     dist.destroy_process_group()
 
 
-def test_two_rank_replicas():
+def _shard_rank(rank, world, port, q, use_gpu):
+    _init(rank, world, port)
+    vs = _views()
+    ws, r, local = shard.dist_env()
+    assert (ws, r, local) == (world, rank, rank)
+    mine = shard.shard_of(vs, r, ws)
+    out = {}
+    if use_gpu:
+        from gorender_gb300 import renderer as R
+        ctx = R.Context(0)
+        sb = shard.ShardedBatch(ctx, vs, mine, autotune=False)
+        sb.run()
+        sb.sync()
+        for k, (i, tpf) in enumerate(zip(mine, sb.view_tpf())):
+            rgba, z = sb.frame(k)
+            out[i] = (_digest(rgba, z), tpf)
+        sb.close()
+        ctx.close()
+    else:
+        from oracle import oracle
+        for i in mine:
+            rgba, z, tpf, st = oracle.draw_scene(vs[i], nthreads=1)
+            assert st == 0
+            out[i] = (_digest(rgba, z), tpf)
+    dist.barrier()
+    q.put((rank, out))
+    dist.destroy_process_group()
+
+
+def _spawn(target, world, *args):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=target, args=(r, world, port, q) + args) for r in range(world)]
     for p in procs:
         p.start()
-    res = sorted(q.get(timeout=300) for _ in procs)
+    res = sorted((q.get(timeout=600) for _ in procs), key=lambda t: t[0])
     for p in procs:
         p.join(timeout=60)
+        assert p.exitcode == 0
+    return res
+
+
+def test_two_rank_replicas():
+    res = _spawn(_replica_rank, 2)
     assert all(r[1] == 0 for r in res)
     assert res[0][2:4] == res[1][2:4]           # identical replicas
     assert res[0][4] == res[1][4] == 2.0         # max over ranks
+
+
+def test_partition_covers_every_view_once_and_balances():
+    vs = scenes.multiview_batch(256, seed=0)
+    costs = [shard.view_cost(s) for s in vs]
+    for world in (1, 2, 3, 4, 8):
+        parts = shard.partition_views(costs, world)
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(len(vs)))
+        loads = [sum(costs[i] for i in p) for p in parts]
+        assert max(loads) - min(loads) <= max(costs) + 1e-6
+        assert parts == shard.partition_views(costs, world)  # deterministic
+    assert shard.partition_views([5.0, 1.0, 1.0], 4) == [[0], [1], [2], []]
+
+
+def _check_union(res, use_gpu):
+    vs = _views()
+    seen = {}
+    for _, out in res:
+        for i, v in out.items():
+            assert i not in seen, f"view {i} rendered twice"
+            seen[i] = v
+    assert sorted(seen) == list(range(len(vs)))
+    from oracle import oracle
+    for i, sc in enumerate(vs):
+        rgba, z, tpf, st = oracle.draw_scene(sc, nthreads=2)
+        assert st == 0 and seen[i] == (_digest(rgba, z), tpf), f"view {i}"
+
+
+def test_two_rank_view_shards_oracle():
+    _check_union(_spawn(_shard_rank, 2, False), False)
+
+
+@pytest.mark.gpu
+def test_two_rank_view_shards_library():
+    _check_union(_spawn(_shard_rank, 2, True), True)
