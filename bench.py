@@ -114,16 +114,74 @@ class ClockSampler:
 
 
 def algorithmic_bytes(scene):
-    """Bytes a frame must move at minimum (vertices, faces, normals, UVs,
-    texels, RGBA8 + fp32 Z written once), split by the kernel that moves them."""
-    V = sum(o.mesh.nv for o in scene.objects)
-    F = sum(o.mesh.nf for o in scene.objects)
+    """Bytes a frame must move at minimum, split by the stage that moves them
+    (the per-view formula of the measurement plan): per object 16 B a vertex
+    position and 12 B a face's indices; flat lighting 16 B a face normal,
+    Gouraud 16 B a vertex normal plus 12 B a face's normal indices; textured
+    faces 24 B of corner UVs; vertex colours 12 B a vertex; then the texels
+    (4 B each) and the framebuffer, RGBA8 + fp32 Z written once (8 B a pixel).
+    Intermediate records (bins, triangle set-up) are not algorithmic."""
+    project = 0
+    lit = bool(scene.flags & 0x08)
     flat = bool(scene.flags & 0x10)
-    textured = any(o.mesh.uv is not None for o in scene.objects)
-    project = 16 * V + 12 * F + (16 * F if flat else 0) + (24 * F if textured else 0)
+    tex_on = bool(scene.flags & 0x20)
+    for o in scene.objects:
+        m = o.mesh
+        project += 16 * m.nv + 12 * m.nf
+        if lit and (flat or m.vnrm is None):
+            project += 16 * m.nf
+        elif lit:
+            project += 16 * m.vnrm.shape[0] + 12 * m.nf
+        textured = tex_on and m.uv is not None and m.tex is not None and bool((m.tex >= 0).any())
+        if textured:
+            project += 24 * m.nf
+        if m.vcolor is not None and not (textured and bool((m.tex >= 0).all())):
+            project += 12 * m.nv
     texels = sum(4 * t.width * t.height for t in scene.textures if t.pixels is not None)
     raster = 8 * scene.width * scene.height + texels
-    return {"project": project, "raster": raster, "frame": project + raster}
+    return {"project": project, "bin": 0, "raster": raster, "frame": project + raster}
+
+
+STAGES = {"project_stage": "k_light + k_vertex + k_cull + k_setup (k_clip starts beside k_setup)",
+          "bin_stage": "k_bin_big + the rest of k_clip",
+          "raster_stage": "k_plan + k_raster + k_resolve (k_clear beside k_raster in a batch)"}
+STAGE_KERNELS = {"project_stage": ["k_light", "k_vertex", "k_cull", "k_setup"],
+                 "bin_stage": ["k_bin_big", "k_clip"],
+                 "raster_stage": ["k_plan", "k_raster", "k_resolve", "k_clear"],
+                 "forward": ["k_raster", "k_diff_shade", "k_diff_vertices"],
+                 "backward": ["k_diff_grad", "k_diff_scatter"]}
+
+
+def _ncu_summary(workload):
+    """Per-workload figures from the committed ncu summaries
+    (profiles/ncu_workloads.json): DRAM traffic per stage and the issue
+    utilisation of each kernel, from one-kernel captures."""
+    path = os.path.join(ROOT, "profiles", "ncu_workloads.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f).get(workload, {})
+
+
+def roofline_of(workload, stage_ms, stage_bytes, stages_desc, launches_per_step=1):
+    """The roofline object of a workload: the stage with the largest share of
+    the step's device time, its algorithmic bytes over its CUDA-event time,
+    against the measured HBM copy bandwidth; traffic and SM issue
+    utilisation of the stage's kernels from the ncu summaries."""
+    top = max(stage_ms, key=lambda k: stage_ms[k])
+    peak, peak_kind = _peaks()
+    ms = stage_ms[top]
+    achieved = stage_bytes[top] / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    ncu = _ncu_summary(workload)
+    issue = {k: v for k, v in ncu.get("issue_active_pct", {}).items()
+             if any(k.startswith(p) for p in STAGE_KERNELS.get(top, []))}
+    traffic = ncu.get("stage_dram_bytes", {}).get(top)
+    return {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": int(stage_bytes[top]),
+            "stage_ms": {k: round(float(v), 5) for k, v in stage_ms.items()},
+            "stages": stages_desc, "sm_issue_active_pct": issue or None,
+            "ncu_source": ncu.get("source")}
 
 
 def dist_env():
@@ -232,12 +290,10 @@ def run_ours(args):
     # k_setup (k_clip starts beside k_setup) | k_bin_big and the rest of
     # k_clip | k_plan + k_raster + k_resolve (k_plan is a one-thread-per-tile
     # scan; k_resolve shades the one view's pixels)
-    names = ["project_stage", "bin_stage", "raster_stage"]
-    top = int(np.argmax(kms))
     ab = algorithmic_bytes(scene)
-    top_bytes = {0: ab["project"], 1: 0, 2: ab["raster"]}[top]
-    peak, peak_kind = _peaks()
-    achieved = top_bytes / (kms[top] * 1e-3) / 1e9 if kms[top] > 0 else 0.0
+    roof = roofline_of("heightfield", dict(zip(["project_stage", "bin_stage", "raster_stage"], kms)),
+                       {"project_stage": ab["project"], "bin_stage": 0, "raster_stage": ab["raster"]}, STAGES)
+    roof["frame_algorithmic_bytes"] = int(ab["frame"])
 
     # end to end through gr_draw with page-locked host outputs
     hp = C.c_void_p()
@@ -276,12 +332,6 @@ def run_ours(args):
     stress = bench_stress(local, args) if not args.skip_batched and ws == 1 else None
     diff = bench_diff(local) if not args.skip_batched and ws == 1 else None
 
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(names[top])
-
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mtris/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_frame, 5),
@@ -294,15 +344,7 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 3), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d.value),
                 "d2h_bytes_per_step": int(d2h.value), "frames": e2e_frames,
                 "ms_per_frame": round(e2e_s * 1e3 / e2e_frames, 4)},
-        "roofline": {"bound": "hbm", "kernel": names[top], "achieved": round(achieved, 2), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": int(top_bytes),
-                     "kernel_ms": {nm: round(float(v), 5) for nm, v in zip(names, kms)},
-                     "stages": {"project_stage": "k_light + k_vertex + k_cull + k_setup",
-                                "bin_stage": "k_bin_big + the rest of k_clip (which starts beside k_setup)",
-                                "raster_stage": "k_plan + k_raster + k_resolve"},
-                     "frame_algorithmic_bytes": int(ab["frame"])},
+        "roofline": roof,
         "parity": None if parity is None else parity["identical"],
         "parity_check": parity,
         "gpu_launches": int(launches_per_frame * args.steps),
@@ -392,6 +434,27 @@ def bench_batched(ctx, args, device, pg=None):
         ctx.event(3)
         ctx.sync()
         t_plain.append(ctx.elapsed_ms(2, 3))
+    kms = np.zeros(3)
+    for _ in range(5):
+        ctx.flush_l2()
+        kms += np.array(sb.batch.profile())
+    kms /= 5
+    per_view = [algorithmic_bytes(sc) for sc in sb.scenes]
+    stage_bytes = {"project_stage": sum(b["project"] for b in per_view), "bin_stage": 0,
+                   "raster_stage": sum(b["raster"] for b in per_view)}
+    if pg:
+        import torch
+        t = torch.tensor(list(kms), dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        kms = t.numpy()
+        for k in ("project_stage", "raster_stage"):
+            t = torch.tensor([float(stage_bytes[k])], dtype=torch.float64)
+            pg.all_reduce(t, op=pg.ReduceOp.SUM)
+            stage_bytes[k] = int(t.item())
+    roof = roofline_of("batch256", dict(zip(["project_stage", "bin_stage", "raster_stage"], kms)), stage_bytes,
+                       STAGES)
+    roof["note"] = ("stages timed outside the graph, one launch sequence per rank; bytes summed over every "
+                    "rank's views, time the slowest rank's")
     sb.run()
     sb.sync()
     launches = ctx.last_launches()
@@ -428,7 +491,7 @@ def bench_batched(ctx, args, device, pg=None):
             "plain_Mtris_per_s": round(faces / (mp * 1e-3) / 1e6, 2),
             "speedup_vs_plain": round(mp / mb, 3), "identical_output": bool(same), "reps": reps,
             "parity": not differing, "views_differing_from_oracle": differing,
-            "tuning": tuning, "kernel_launches_per_batch": launches}
+            "tuning": tuning, "kernel_launches_per_batch": launches, "roofline": roof}
 
 
 def bench_diff(device):
@@ -483,6 +546,10 @@ def bench_diff(device):
         tf.append(ctx.elapsed_ms(6, 7))
         tb.append(ctx.elapsed_ms(7, 8))
     mf, mb = statistics.median(tf), statistics.median(tb)
+    roof = roofline_of("diff64", {"forward": mf, "backward": mb}, diff_bytes(sc, views),
+                       {"forward": "visibility pass (the frame kernels in face-id mode) + k_diff_vertices + "
+                                   "k_diff_tables + k_diff_shade",
+                        "backward": "k_diff_grad + k_diff_scatter"})
     d.close()
     for x in p + q + g + [target, zeros]:
         x.free()
@@ -490,7 +557,23 @@ def bench_diff(device):
     return {"workload": "diff-icosphere6-81920f-64views-512x512-tex256", "views": 64, "faces": sc.mesh.nf,
             "pixels": npx, "forward_ms": round(mf, 4), "backward_ms": round(mb, 4),
             "backward_over_forward": round(mb / mf, 3), "views_per_s": round(64 / ((mf + mb) * 1e-3), 1),
-            "loss": loss, "reps": reps, "l2": "flushed between iterations"}
+            "loss": loss, "reps": reps, "l2": "flushed between iterations", "roofline": roof}
+
+
+def diff_bytes(sc, views):
+    """Algorithmic bytes of one differentiable step.  Forward, per view: the
+    parameter positions (16 B a vertex), indices (12 B a face) and vertex
+    colours (12 B a vertex), then per pixel the 16-byte record the backward
+    pass reads and the 16-byte target; once, the fp32 texture (16 B a texel).
+    Backward: per pixel the record and the target again (32 B), the
+    parameters read once and their gradients written once (positions 16 B,
+    colours 12 B a vertex, texels 16 B)."""
+    V, F = sc.mesh.nv, sc.mesh.nf
+    texels = sc.tex.shape[0] * sc.tex.shape[1]
+    px = sum(w * h for w, h, _, _, _ in views)
+    fwd = len(views) * (16 * V + 12 * F + 12 * V) + 32 * px + 16 * texels
+    bwd = 32 * px + 2 * (16 * V + 12 * V + 16 * texels) + 12 * F
+    return {"forward": fwd, "backward": bwd}
 
 
 def bench_present(ctx, up, scene, frames):
@@ -553,12 +636,23 @@ def bench_stress(device, args):
         ctx.sync()
         t.append(ctx.elapsed_ms(4, 5))
     ms = statistics.median(t)
+    kms = np.zeros(3)
+    buf = (C.c_float * 3)()
+    for _ in range(10):
+        N.check(N.lib().gr_draw_profiled(ctx.handle, up.items, n, C.byref(up.params), None, None, buf))
+        kms += np.array(buf[:])
+        ctx.flush_l2()
+    kms /= 10
+    ab = algorithmic_bytes(sc)
+    roof = roofline_of("icospheres", dict(zip(["project_stage", "bin_stage", "raster_stage"], kms)),
+                       {"project_stage": ab["project"], "bin_stage": 0, "raster_stage": ab["raster"]}, STAGES)
+    roof["frame_algorithmic_bytes"] = int(ab["frame"])
     rgba, z, tpf = up.render()
     chk = frame_parity(sc, rgba, z, tpf)
     out = {"workload": "icospheres-64obj-1920x1080-gouraud-vertex-rgb", "faces": sc.num_triangles,
            "parity": chk["identical"], "parity_check": chk,
            "ms_per_frame": round(ms, 4), "Mtris_per_s": round(sc.num_triangles / (ms * 1e-3) / 1e6, 2),
-           "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0]}
+           "frames": frames, "tile_size": ctx.tuning()[0], "slice_cost": ctx.raster()[0], "roofline": roof}
     ctx.close()
     return out
 

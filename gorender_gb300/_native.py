@@ -40,7 +40,7 @@ EXPORTS = [
     "gr_context_autotune", "gr_diff_create", "gr_diff_forward", "gr_diff_backward", "gr_diff_buffers",
     "gr_diff_destroy", "gr_fog", "gr_context_set_fog", "gr_renderer_fog", "gr_presenter_create",
     "gr_presenter_frame", "gr_presenter_flush", "gr_presenter_destroy", "gr_device_alloc", "gr_device_free",
-    "gr_copy",
+    "gr_copy", "gr_batch_profile",
 ]
 
 
@@ -183,6 +183,7 @@ def lib() -> C.CDLL:
             "gr_device_alloc": [vp, C.c_int64, C.POINTER(vp)],
             "gr_device_free": [vp, vp],
             "gr_copy": [vp, vp, vp, C.c_int64],
+            "gr_batch_profile": [vp, fp],
         }
         for name, args in sig.items():
             f = getattr(L, name)

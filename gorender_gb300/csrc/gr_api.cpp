@@ -1326,6 +1326,30 @@ int32_t gr_batch_sync(gr_batch* b) {
   return fail(GR_ERR_OUT_OF_MEMORY, "batch buffers kept overflowing after resizing");
 }
 
+int32_t gr_batch_profile(gr_batch* b, float* stage_ms3) {
+  if (!b || !stage_ms3) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  gr_context* c = b->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  const int nv = (int)b->views.size();
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    Prepared pr;
+    int32_t st = prepare(c, b->vin.data(), nv, b->items.data(), (int)b->items.size(), true, pr);
+    if (st) return st;
+    void* ev[4] = {c->events[60], c->events[61], c->events[62], c->events[63]};
+    if ((st = launch(c, pr.a, ev))) return st;
+    CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int32_t err;
+    const int rerun = check_result(c, *c->h_result, &err);
+    if (err) return err;
+    if (rerun) continue;
+    for (int k = 0; k < 3; ++k) CK(cudaEventElapsedTime(&stage_ms3[k], c->events[60 + k], c->events[61 + k]));
+    return GR_OK;
+  }
+  return fail(GR_ERR_OUT_OF_MEMORY, "batch buffers kept overflowing after resizing");
+}
+
 int32_t gr_batch_tuning(gr_batch* b, int32_t* tile_size, int32_t* slice_cost, int32_t* raster_waves,
                         int32_t* bin_capacity, float* tuned_ms) {
   if (!b) return fail(GR_ERR_INVALID_ARGUMENT, "batch is NULL");

@@ -494,6 +494,13 @@ class Batch:
         return {"tile_size": t.value, "slice_cost": s.value, "raster_waves": w.value,
                 "bin_capacity": b.value, "tuned_ms": ms.value}
 
+    def profile(self) -> Tuple[float, float, float]:
+        """Stage durations in ms (project, multi-tile binning, raster) of one
+        run of the batch's frame outside its graph (gr_batch_profile)."""
+        ms = (C.c_float * 3)()
+        N.check(N.lib().gr_batch_profile(self._h, ms))
+        return float(ms[0]), float(ms[1]), float(ms[2])
+
     def view_tpf(self):
         out = (C.c_int64 * self.nviews)()
         N.check(N.lib().gr_context_view_tpf(self.ctx.handle, out, self.nviews))

@@ -174,6 +174,10 @@ int32_t gr_batch_sync(gr_batch* batch);
 int32_t gr_batch_tuning(gr_batch* batch, int32_t* tile_size, int32_t* slice_cost,
                         int32_t* raster_waves, int32_t* bin_capacity, float* tuned_ms);
 int32_t gr_batch_destroy(gr_batch* batch);
+/* The batch's frame once outside its graph, at its tuning, with CUDA events
+ * between the stages (as gr_draw_profiled): stage_ms3 receives the project,
+ * multi-tile binning and raster stage durations.  Synchronous. */
+int32_t gr_batch_profile(gr_batch* batch, float* stage_ms3);
 
 /* ---- host math (R1: stays on the host, restated from matrix.go) ---- */
 typedef struct {
