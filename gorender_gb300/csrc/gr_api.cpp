@@ -1688,7 +1688,7 @@ struct gr_diff {
   unsigned* bbox_done = nullptr;
   double* d_acc = nullptr;              // loss, light gradient x 3
   double* d_partials = nullptr;         // per-warp sums (kDiffSlots x 4), zero when idle
-  float* d_gface = nullptr;             // per-face corner gradient sums (nf x 18), zero when idle
+  float* d_gface = nullptr;             // per-face corner gradient sums (nf x 3 x 8), zero when idle
   double* h_acc = nullptr;              // pinned
   gr_diff_params last{};                // parameters of the last forward
   const float* last_target = nullptr;
@@ -1870,8 +1870,8 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st) st = dev_alloc(&d->d_partials, (size_t)kDiffSlots * 4);
   if (!st && cudaMemsetAsync(d->d_partials, 0, sizeof(double) * kDiffSlots * 4, c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff partials");
-  if (!st) st = dev_alloc(&d->d_gface, (size_t)d->nf * 18);
-  if (!st && cudaMemsetAsync(d->d_gface, 0, sizeof(float) * 18 * (size_t)d->nf, c->stream) != cudaSuccess)
+  if (!st) st = dev_alloc(&d->d_gface, (size_t)d->nf * 24);
+  if (!st && cudaMemsetAsync(d->d_gface, 0, sizeof(float) * 24 * (size_t)d->nf, c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff face sums");
   if (!st && cudaMallocHost((void**)&d->h_acc, 4 * sizeof(double)) != cudaSuccess) {
     d->h_acc = nullptr;
@@ -1963,6 +1963,8 @@ int32_t gr_diff_backward(gr_diff* d, gr_diff_grads* g) {
       (g->texture && !is_device_ptr(g->texture)))
     return fail(GR_ERR_INVALID_ARGUMENT, "gradient buffers must be device pointers");
   if (d->last.texture && !g->texture) return fail(GR_ERR_INVALID_ARGUMENT, "texture gradient buffer is NULL");
+  if (g->texture && ((uintptr_t)g->texture & 15u))
+    return fail(GR_ERR_INVALID_ARGUMENT, "texture gradient buffer must be 16-byte aligned");
   gr_context* c = d->ctx;
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));

@@ -271,8 +271,9 @@ struct DiffArgs {
   float* g_tex;                     // th x tw x 4
   double* g_light;                  // 3, accumulated
   double* partials;                 // kDiffSlots x {loss, light x, y, z}: per-warp sums, zero when idle
-  float* g_face;                    // nf x 3 corners x {colour r, g, b, position x, y, z}: the
-                                    // backward's per-face sums before k_diff_scatter (zero when idle)
+  float* g_face;                    // nf x 3 corners x {colour r, g, b, position x, y, z, 0, 0}: the
+                                    // backward's per-face sums before k_diff_scatter (zero when idle),
+                                    // two float4 a corner
 };
 constexpr int kDiffSlots = 1024;     // slots of DiffArgs::partials
 

@@ -394,7 +394,8 @@ typedef struct {
 typedef struct {
   float* positions;      /* DEVICE num_vertices x 4 (w gradient 0), overwritten */
   float* vertex_colors;  /* DEVICE num_vertices x 3, overwritten */
-  float* texture;        /* DEVICE texture_height x texture_width x 4, overwritten (or NULL) */
+  float* texture;        /* DEVICE texture_height x texture_width x 4, overwritten (or NULL);
+                            16-byte aligned (texels are accumulated as float4) */
   double light[3];       /* written */
 } gr_diff_grads;
 

@@ -125,6 +125,15 @@ def test_backward_is_repeatable(small):
     assert np.allclose(gl, small.g_light, rtol=1e-5)
 
 
+def test_misaligned_texture_gradient_rejected(small):
+    """Texel gradients are accumulated as float4: a texture gradient buffer
+    that is not 16-byte aligned is refused before any kernel runs."""
+    big = torch.empty(small.g[2].numel() + 4, device="cuda")
+    with pytest.raises(gr.GrError) as e:
+        small.diff.backward(small.g[0].data_ptr(), small.g[1].data_ptr(), big.data_ptr() + 4)
+    assert e.value.code == R.N.GR_ERR_INVALID_ARGUMENT and "aligned" in str(e.value)
+
+
 def test_full_size_workload(oracle_lib):
     """64 views at 512x512 of the 81,920-face icosphere (the benchmark workload)."""
     run = Run(dc.small_case(views=64, size=512, level=6, tex_size=256, seed=0))
