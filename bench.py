@@ -142,13 +142,16 @@ def algorithmic_bytes(scene):
     return {"project": project, "bin": 0, "raster": raster, "frame": project + raster}
 
 
-STAGES = {"project_stage": "k_light + k_vertex + k_cull + k_setup (k_clip starts beside k_setup)",
-          "bin_stage": "k_bin_big + the rest of k_clip",
-          "raster_stage": "k_plan + k_raster + k_resolve (k_clear beside k_raster in a batch)"}
-STAGE_KERNELS = {"project_stage": ["k_light", "k_vertex", "k_cull", "k_setup"],
-                 "bin_stage": ["k_bin_big", "k_clip"],
+# Stages of the profiled pass (CUDA events between them; every kernel on the
+# context stream, so k_clip runs inside the project stage here, while a graph
+# replay runs it beside k_setup and k_bin_big).
+STAGES = {"project_stage": "k_light + k_vertex + k_cull + k_clip + k_setup",
+          "bin_stage": "k_bin_big (+ k_overlay)",
+          "raster_stage": "k_plan + k_raster + k_resolve (one view) or k_plan + k_clear + k_raster (a batch)"}
+STAGE_KERNELS = {"project_stage": ["k_light", "k_vertex", "k_cull", "k_clip", "k_setup"],
+                 "bin_stage": ["k_bin_big", "k_overlay"],
                  "raster_stage": ["k_plan", "k_raster", "k_resolve", "k_clear"],
-                 "forward": ["k_raster", "k_diff_shade", "k_diff_vertices"],
+                 "forward": ["k_diff_vertices", "k_diff_tables", "k_diff_shade"],
                  "backward": ["k_diff_grad", "k_diff_scatter"]}
 
 
@@ -176,11 +179,14 @@ def roofline_of(workload, stage_ms, stage_bytes, stages_desc, launches_per_step=
     issue = {k: v for k, v in ncu.get("issue_active_pct", {}).items()
              if any(k.startswith(p) for p in STAGE_KERNELS.get(top, []))}
     traffic = ncu.get("stage_dram_bytes", {}).get(top)
+    stage_issue = ncu.get("stage_issue_active_pct_time_weighted", {}).get(top)
     return {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": int(stage_bytes[top]),
             "stage_ms": {k: round(float(v), 5) for k, v in stage_ms.items()},
-            "stages": stages_desc, "sm_issue_active_pct": issue or None,
+            "stages": stages_desc,
+            "sm_issue_active": None if stage_issue is None else {
+                "stage_pct_of_peak": stage_issue, "frac": round(stage_issue / 100.0, 4), "per_kernel_pct": issue},
             "ncu_source": ncu.get("source")}
 
 

@@ -58,6 +58,9 @@ def run_frames(args):
 def run_batch(args):
     vs = scenes.multiview_batch(256, seed=0)
     ctx = R.Context(args.device)
+    if args.tile or args.slice:  # the autotuner's choice for this batch, without running it
+        ctx.set_tuning(args.tile, args.bins)
+        N.check(N.lib().gr_context_set_raster(ctx.handle, args.slice, 0))
     views, entries, bufs = [], [], []
     for v, sc in enumerate(vs):
         up = R.UploadedScene(ctx, sc)
@@ -117,6 +120,7 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="run the library autotuner first")
     ap.add_argument("--tile", type=int, default=0, help="raster tile size (16 or 32; 0 keeps the default)")
     ap.add_argument("--slice", type=int, default=0, help="raster cost per slice (0 keeps the default)")
+    ap.add_argument("--bins", type=int, default=0, help="tile bin capacity (0 keeps the default)")
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args()
     from gorender_gb300 import build
