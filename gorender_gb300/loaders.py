@@ -20,8 +20,9 @@
   PNG specification) and convert each pixel as color.RGBAModel.Convert does,
   i.e. alpha-premultiplied 8-bit RGBA: for non-premultiplied input,
   out = ((c * 257 * a) // 255) >> 8 at 8 bits and ((c16 * a16) // 65535) >> 8 at
-  16 bits.  Power-of-two sizes select the fast (mask) sampler.  JPEG is not
-  decoded here.
+  16 bits.  Power-of-two sizes select the fast (mask) sampler.  JPEG (which
+  texture.go:6 also registers) is rejected with a clear error: Go's decoder
+  could not be matched bit for bit against any Go output here.
 * Scene manifests: every mesh of the manifest is its file's first mesh
   (LoadMeshFile(..., true)); its faces all take the manifest's texture (with
   textureScale when non-zero) or the solid (200, 200, 200, 255) colour; object
@@ -276,6 +277,8 @@ def load_texture(path: str, scale: float = 1.0) -> TextureData:
     """LoadTextureFile + NewImageTexture: the fast sampler for power-of-two sizes."""
     with open(path, "rb") as f:
         data = f.read()
+    if data[:3] == b"\xff\xd8\xff":
+        raise ValueError(f"{path}: JPEG textures are not decoded here (convert the texture to PNG)")
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError(f"{path}: only PNG textures are decoded here")
     return TextureData.image(decode_png(data), scale=float(np.float32(scale)))

@@ -224,3 +224,10 @@ def test_reference_sample_models_load():
     assert (px[..., :3] <= px[..., 3:]).all()
     meshes, texs = loaders.load_obj(os.path.join(REF_MODELS, "suzanne.obj"))
     assert meshes[0].nv == 507 and meshes[0].nf == 967 and texs == []
+
+
+def test_jpeg_texture_rejected_clearly(tmp_path):
+    p = tmp_path / "t.jpg"
+    p.write_bytes(b"\xff\xd8\xff\xe0" + bytes(60))
+    with pytest.raises(ValueError, match="JPEG"):
+        loaders.load_texture(str(p))
