@@ -615,7 +615,7 @@ def bench_present(ctx, up, scene, frames):
 
 
 def bench_stress(device, args):
-    """The 64-icosphere 1920x1080 scene (3.6M faces, per-vertex colours) on a
+    """The 64-icosphere 1920x1080 scene (5.0M faces, per-vertex colours) on a
     context of its own: device-timed frames after the autotuner, L2 flushed
     between frames."""
     import ctypes as C

@@ -371,12 +371,29 @@ def scene_heightfield_1280x720(n: int = 317) -> SceneData:
                      DEFAULT_FLAGS | FLAT_SHADING)
 
 
-def scene_icospheres_1920x1080(count: int = 64, seed: int = 0, levels=(5, 6)) -> SceneData:
+def scene_icospheres_1920x1080(count: int = 64, seed: int = 0, levels=(5, 6),
+                               total_faces: Optional[int] = None) -> SceneData:
     """Small-triangle stress: ``count`` icospheres of level 5 or 6 placed
     uniformly in a 40-unit cube with scale U[0.2, 2], per-vertex RGB colours
-    U[0,1] (extension), Gouraud shading, 1920x1080."""
+    U[0,1] (extension), Gouraud shading, 1920x1080.
+
+    The configuration asks for about 5 M faces in all: a level-5 sphere has
+    20,480 faces and a level-6 one 81,920, so an even mix of 64 would give
+    3.3 M.  With ``total_faces`` (5,000,000 by default for levels 5 and 6)
+    and two levels, the number of higher-level spheres is the one whose total
+    is nearest to it (60 of 64: 4,997,120 faces) and a seeded permutation
+    picks which; otherwise (the smaller test scenes) each level is drawn at
+    random."""
+    if total_faces is None and tuple(levels) == (5, 6):
+        total_faces = 5_000_000
     rng = SplitMix64(seed)
     lv = rng.integers(count, 0, len(levels))
+    if total_faces is not None and len(levels) == 2:
+        f_lo, f_hi = 20 * 4 ** levels[0], 20 * 4 ** levels[1]
+        n_hi = int(min(count, max(0, round((total_faces - count * f_lo) / (f_hi - f_lo)))))
+        order = np.argsort(SplitMix64(seed * 1000 + 7).uniform(count), kind="stable")
+        lv = np.zeros(count, np.int64)
+        lv[order[:n_hi]] = 1
     meshes = {}
     objs = []
     for k in range(count):

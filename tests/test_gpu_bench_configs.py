@@ -3,7 +3,7 @@
 * the 199,712-face heightfield at 1280x720 after the library autotuner, and
   forced to the tuning the bench has reported (16x16 tiles, raster slice cost
   4096, bin capacity 1024);
-* the 64-icosphere 1920x1080 frame with per-vertex colours (3.6 M faces), at
+* the 64-icosphere 1920x1080 frame with per-vertex colours (5.0 M faces), at
   the default tuning and after the autotuner;
 * every view of the 256-view batch (its CUDA graph, autotuned) against the
   oracle's frame of that view alone.
