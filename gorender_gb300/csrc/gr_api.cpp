@@ -105,6 +105,7 @@ struct gr_context {
 
   TriRaster* rast = nullptr;
   TriShade* shade = nullptr;
+  TriUV* suv = nullptr;
   TriWide* wide = nullptr;
   TriColor* tcol = nullptr;
   uint32_t rec_cap = 0;
@@ -273,10 +274,11 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
   want_rec = std::min<uint64_t>(want_rec, (uint64_t)kMaxFan * faces + 1024);
   if (want_rec > c->rec_cap) {
     if ((st = sync())) return st;
-    dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
+    dev_free(c->rast); dev_free(c->shade); dev_free(c->suv); dev_free(c->wide); dev_free(c->tcol);
     c->rec_cap = 0;
     if ((st = dev_alloc(&c->rast, want_rec)) || (st = dev_alloc(&c->shade, want_rec)) ||
-        (st = dev_alloc(&c->wide, want_rec)) || (st = dev_alloc(&c->tcol, want_rec)))
+        (st = dev_alloc(&c->suv, want_rec)) || (st = dev_alloc(&c->wide, want_rec)) ||
+        (st = dev_alloc(&c->tcol, want_rec)))
       return st;
     c->rec_cap = (uint32_t)want_rec;
   }
@@ -610,6 +612,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.num_tex = (int)c->texs.size();
   a.rast = c->rast;
   a.shade = c->shade;
+  a.suv = c->suv;
   a.wide = c->wide;
   a.tcol = c->tcol;
   a.rec_of_key = c->rec_of_key;
@@ -711,7 +714,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
 // Identity of every context buffer a captured graph refers to: a graph whose
 // signature no longer matches must be captured again before it runs.
 uint64_t buffers_signature(const gr_context* c) {
-  const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->wide, (uintptr_t)c->tcol,
+  const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->suv, (uintptr_t)c->wide, (uintptr_t)c->tcol,
                           (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->gkey,
                           (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->kept, c->kept_cap, (uintptr_t)c->big, (uintptr_t)c->vlight,
                           (uintptr_t)c->vclip, (uintptr_t)c->vscr,
@@ -869,7 +872,7 @@ int32_t gr_context_destroy(gr_context* c) {
   for (auto& t : c->texs) if (t.px) cudaFree(t.px);
   dev_free(c->d_texs); dev_free(c->d_tables);
   if (c->h_tables) cudaFreeHost(c->h_tables);
-  dev_free(c->rast); dev_free(c->shade); dev_free(c->wide); dev_free(c->tcol);
+  dev_free(c->rast); dev_free(c->shade); dev_free(c->suv); dev_free(c->wide); dev_free(c->tcol);
   dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->kept); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);

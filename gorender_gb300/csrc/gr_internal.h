@@ -104,15 +104,24 @@ struct alignas(16) TriWide {
   long long pad;
 };
 
-// Shading inputs of one binned triangle (48 bytes).
+// Shading inputs of one binned triangle, in two arrays so that each frame
+// writes only what its triangles use, in whole 32-byte sectors: the
+// intensities and texture slot of every triangle (16 bytes) and, for
+// textured triangles only, u/W and v/W per vertex (32 bytes).
 struct alignas(16) TriShade {
-  float u0w, v0w, u1w, v1w, u2w, v2w; // u/W and v/W per vertex (rasterizer.go:132-137)
   float i0, i1, i2;                   // light intensity per vertex
-  int tex;                            // texture slot; -1 = faceColor; -2 = vertex colour
+  int tex;                            // texture slot; -1 = faceColor; -2 = vertex colour from
+                                      // TriColor (clipped fans); -3 = vertex colour of kept face r,
+                                      // gathered again from the mesh (no TriColor written)
+};
+struct alignas(16) TriUV {
+  float u0w, v0w, u1w, v1w, u2w, v2w; // u/W and v/W per vertex (rasterizer.go:132-137)
   float pad[2];
 };
 
-// Per-vertex RGB of a triangle (vertex-colour extension), 3 x 3 floats.
+// Per-vertex RGB of a clipped fan triangle (vertex-colour extension), 3 x 3
+// floats; the whole faces k_cull keeps are shaded from the mesh's own
+// vertex colours instead (TriShade::tex == -3).
 struct TriColor {
   float c[9];
 };
@@ -175,6 +184,7 @@ struct FrameArgs {
   int num_tex;
   TriRaster* rast;
   TriShade* shade;
+  TriUV* suv;                       // read only for textured triangles (TriShade::tex >= 0)
   TriWide* wide;
   TriColor* tcol;
   uint32_t* rec_of_key;             // order key -> record index

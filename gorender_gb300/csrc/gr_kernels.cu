@@ -467,7 +467,7 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
 
 // Writes record r of a set-up triangle (raster part, int64 edges, shading).
 __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Setup& s, const SV& q0, const SV& q1,
-                                             const SV& q2, int tex, uint32_t okey) {
+                                             const SV& q2, int tex, uint32_t okey, bool from_kept = false) {
   s.r.key = okey | (s.wide ? 0x80000000u : 0u);
   const int4* src = reinterpret_cast<const int4*>(&s.r);
   int4* dst = reinterpret_cast<int4*>(a.rast + r);
@@ -478,21 +478,13 @@ __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Set
 #pragma unroll
     for (int q = 0; q < 5; ++q) wd[q] = ws[q];
   }
-  TriShade sh;
-  if (tex >= 0) {  // read by the shading only through a texture
-    sh.u0w = fd(q0.u, q0.W); sh.v0w = fd(q0.v, q0.W);  // rasterizer.go:132-137
-    sh.u1w = fd(q1.u, q1.W); sh.v1w = fd(q1.v, q1.W);
-    sh.u2w = fd(q2.u, q2.W); sh.v2w = fd(q2.v, q2.W);
-  } else {
-    sh.u0w = sh.v0w = sh.u1w = sh.v1w = sh.u2w = sh.v2w = 0.0f;
+  reinterpret_cast<float4*>(a.shade)[r] = make_float4(q0.in, q1.in, q2.in, __int_as_float(tex == -2 && from_kept ? -3 : tex));
+  if (tex >= 0) {  // read by the shading only through a texture (rasterizer.go:132-137)
+    float4* uv = reinterpret_cast<float4*>(a.suv + r);
+    uv[0] = make_float4(fd(q0.u, q0.W), fd(q0.v, q0.W), fd(q1.u, q1.W), fd(q1.v, q1.W));
+    uv[1] = make_float4(fd(q2.u, q2.W), fd(q2.v, q2.W), 0.0f, 0.0f);
   }
-  sh.i0 = q0.in; sh.i1 = q1.in; sh.i2 = q2.in;
-  sh.tex = tex;
-  sh.pad[0] = sh.pad[1] = 0.0f;
-  const float4* ss = reinterpret_cast<const float4*>(&sh);
-  float4* sd = reinterpret_cast<float4*>(a.shade + r);
-  sd[0] = ss[0]; sd[1] = ss[1]; sd[2] = ss[2];
-  if (tex == -2) {
+  if (tex == -2 && !from_kept) {
     TriColor* c = a.tcol + r;
     c->c[0] = q0.r; c->c[1] = q0.g; c->c[2] = q0.b;
     c->c[3] = q1.r; c->c[4] = q1.g; c->c[5] = q1.b;
@@ -802,7 +794,7 @@ __global__ void __launch_bounds__(kProjectThreads, kSetupCtasPerSm) k_setup(cons
     uint32_t tx0 = 0, tx1 = 0, ty0 = 0, ty1 = 0;
     int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
     if (ok) {
-      write_record(a, r, s, s0, s1, s2, tex, okey);
+      write_record(a, r, s, s0, s1, s2, tex, okey, true);
       pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
       tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
       tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
@@ -1388,15 +1380,33 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
     const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
     uint32_t c;
     if (s.tex >= 0) {
-      const float u = fd(fa(fa(fm(al, s.u0w), fm(be, s.u1w)), fm(ga, s.u2w)), z);
-      const float v = fd(fa(fa(fm(al, s.v0w), fm(be, s.v1w)), fm(ga, s.v2w)), z);
+      const TriUV q = a.suv[r];
+      const float u = fd(fa(fa(fm(al, q.u0w), fm(be, q.u1w)), fm(ga, q.u2w)), z);
+      const float v = fd(fa(fa(fm(al, q.v0w), fm(be, q.v1w)), fm(ga, q.v2w)), z);
       c = color_intensity(tex_sample(a.texs[s.tex], u, v), I);
-    } else if (s.tex == -2) {
-      const TriColor& tc = a.tcol[r];
+    } else if (s.tex == -2 || s.tex == -3) {
+      float cc[9];
+      if (s.tex == -2) {
+        const TriColor& tc = a.tcol[r];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cc[q] = tc.c[q];
+      } else {
+        // a kept face: record r is kept face r, whose vertex colours are read
+        // again through the kept list, the same floats k_setup saw (not
+        // writing them as a record: the 5 M-face stress frame 0.403 -> 0.367 ms)
+        const uint2 e = a.kept[r];
+        const DevItem& it = a.items[e.x];
+        const int* vi = it.vidx + 3 * (size_t)e.y;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float* cp = it.vcol + 3 * (size_t)__ldg(vi + k);
+          cc[3 * k] = __ldg(cp); cc[3 * k + 1] = __ldg(cp + 1); cc[3 * k + 2] = __ldg(cp + 2);
+        }
+      }
       uint32_t ch[3];
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        const float cq = fa(fa(fm(al, tc.c[q]), fm(be, tc.c[3 + q])), fm(ga, tc.c[6 + q]));
+        const float cq = fa(fa(fm(al, cc[q]), fm(be, cc[3 + q])), fm(ga, cc[6 + q]));
         ch[q] = go_u8(fm(fm(cq, 255.0f), I));
       }
       c = ch[0] | (ch[1] << 8) | (ch[2] << 16) | 0xFF000000u;

@@ -64,7 +64,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
-  size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, wide, tcol, keys, bins, bin_count, tile_cost, big, clip, kept,
+  size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, suv, wide, tcol, keys, bins, bin_count, tile_cost, big, clip, kept,
       vlight, vclip, vscr, gkey, tile_done, work, result, check, end;
 };
 
@@ -80,6 +80,7 @@ constexpr Layout make_layout() {
   l.empty = o; o += up256(sizeof(uint2) * kTiles);
   l.rast = o; o += up256(sizeof(TriRaster) * kRecCap);
   l.shade = o; o += up256(sizeof(TriShade) * kRecCap);
+  l.suv = o; o += up256(sizeof(TriUV) * kRecCap);
   l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
   l.tcol = o; o += up256(sizeof(TriColor) * kRecCap);
   l.keys = o; o += up256(sizeof(uint32_t) * kKeyCap);
@@ -295,6 +296,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.num_tex = num_textures;
   a.rast = (TriRaster*)(base + kLayout.rast);
   a.shade = (TriShade*)(base + kLayout.shade);
+  a.suv = (TriUV*)(base + kLayout.suv);
   a.wide = (TriWide*)(base + kLayout.wide);
   a.tcol = (TriColor*)(base + kLayout.tcol);
   a.rec_of_key = (uint32_t*)(base + kLayout.keys);
