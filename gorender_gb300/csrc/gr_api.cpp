@@ -103,7 +103,7 @@ struct gr_context {
   bool stage_used[kStageSlots] = {};
   int stage_slot = 0;
 
-  TriRaster* rast = nullptr;
+  TriPacked* rast = nullptr;
   TriShade* shade = nullptr;
   TriUV* suv = nullptr;
   TriWide* wide = nullptr;

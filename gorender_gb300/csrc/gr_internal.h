@@ -84,7 +84,8 @@ struct DevItem {
   int vert_block_base;              // first k_vertex block of this item
 };
 
-// Raster setup of one binned triangle (64 bytes).  For "narrow" triangles
+// Raster setup of one binned triangle (64 bytes, in registers and shared
+// memory; stored as a TriPacked).  For "narrow" triangles
 // (all screen coordinates within +-2^14) the three adjusted edge functions
 // E(x,y) = a*x + b*y + c evaluate exactly in int32 over the screen.
 struct alignas(16) TriRaster {
@@ -98,11 +99,26 @@ struct alignas(16) TriRaster {
 };
 static_assert(sizeof(TriRaster) == 64, "TriRaster layout");
 
-// int64 edge coefficients of a "wide" triangle (wraparound arithmetic).
+// int64 edge coefficients of a "wide" triangle (wraparound arithmetic) and
+// its pixel box (its corners do not fit a TriPacked).
 struct alignas(16) TriWide {
   long long a01, b01, c01, a12, b12, c12, a20, b20, c20;
-  long long pad;
+  int16_t bx0, bx1, by0, by1;
 };
+
+// The raster record of one binned triangle as stored (32 bytes): what the
+// raster needs of a narrow triangle follows from its integer screen corners
+// (|coordinate| < 2^14), its three W's and its order key -- the edge
+// functions, the top-left adjustment, the sum and the clamped pixel box are
+// recomputed where the record is read (unpack_tri).  A wide triangle keeps
+// its sum here and its int64 edges and box in TriWide.
+struct alignas(16) TriPacked {
+  int16_t x0, y0, x1, y1, x2, y2;   // narrow triangles only
+  uint32_t key;                     // bit 31: wide; bits 0..30: face*8 + fan + 1
+  float w0, w1, w2;                 // clip-space W of the vertices (the rasteriser's z)
+  float sumf;                       // wide triangles only: float32(E01+E12+E20)
+};
+static_assert(sizeof(TriPacked) == 32, "TriPacked layout");
 
 // Shading inputs of one binned triangle, in two arrays so that each frame
 // writes only what its triangles use, in whole 32-byte sectors: the
@@ -182,7 +198,7 @@ struct FrameArgs {
   const DevItem* items;
   const DevTex* texs;
   int num_tex;
-  TriRaster* rast;
+  TriPacked* rast;
   TriShade* shade;
   TriUV* suv;                       // read only for textured triangles (TriShade::tex >= 0)
   TriWide* wide;

@@ -314,12 +314,47 @@ __device__ __forceinline__ bool setup_tri(const SV& p0, const SV& p1, const SV& 
     s.w.a01 = (long long)a01; s.w.b01 = (long long)b01; s.w.c01 = (long long)c01;
     s.w.a12 = (long long)a12; s.w.b12 = (long long)b12; s.w.c12 = (long long)c12;
     s.w.a20 = (long long)a20; s.w.b20 = (long long)b20; s.w.c20 = (long long)c20;
-    s.w.pad = 0;
+    s.w.bx0 = s.w.bx1 = s.w.by0 = s.w.by1 = 0;
     s.r.a01 = s.r.b01 = s.r.c01 = s.r.a12 = s.r.b12 = s.r.c12 = s.r.a20 = s.r.b20 = s.r.c20 = 0;
     s.r.sumf = __ll2float_rn((long long)sum);
     s.wide = true;
   }
   return true;
+}
+
+// The raster record r as the raster, binning and resolve use it, rebuilt from
+// its stored TriPacked for a view of W x H pixels: for a narrow triangle the
+// same integer arithmetic as setup_tri, from the same corners, so the same
+// values.
+__device__ __forceinline__ TriRaster unpack_tri(const FrameArgs& a, uint32_t r, int W, int H) {
+  const int4* src = reinterpret_cast<const int4*>(a.rast + r);
+  const int4 c = src[0];
+  const float4 w = reinterpret_cast<const float4*>(src)[1];
+  TriRaster t;
+  t.key = (uint32_t)c.w;
+  t.w0 = w.x; t.w1 = w.y; t.w2 = w.z;
+  if (t.key & 0x80000000u) {
+    const TriWide& wd = a.wide[r];
+    t.a01 = t.b01 = t.c01 = t.a12 = t.b12 = t.c12 = t.a20 = t.b20 = t.c20 = 0;
+    t.sumf = w.w;
+    t.bx0 = wd.bx0; t.bx1 = wd.bx1; t.by0 = wd.by0; t.by1 = wd.by1;
+    return t;
+  }
+  const int x0 = (int16_t)(c.x & 0xFFFF), y0 = (int16_t)((uint32_t)c.x >> 16);
+  const int x1 = (int16_t)(c.y & 0xFFFF), y1 = (int16_t)((uint32_t)c.y >> 16);
+  const int x2 = (int16_t)(c.z & 0xFFFF), y2 = (int16_t)((uint32_t)c.z >> 16);
+  t.a01 = y0 - y1; t.b01 = x1 - x0; t.c01 = x0 * y1 - x1 * y0;
+  t.a12 = y1 - y2; t.b12 = x2 - x1; t.c12 = x1 * y2 - x2 * y1;
+  t.a20 = y2 - y0; t.b20 = x0 - x2; t.c20 = x2 * y0 - x0 * y2;
+  if (!keeps_edge(t.a01, t.b01)) t.c01 -= 1;
+  if (!keeps_edge(t.a12, t.b12)) t.c12 -= 1;
+  if (!keeps_edge(t.a20, t.b20)) t.c20 -= 1;
+  t.sumf = __ll2float_rn((long long)t.c01 + (long long)t.c12 + (long long)t.c20);
+  t.bx0 = (int16_t)max(min(min(x0, x1), x2), 0);
+  t.bx1 = (int16_t)min(max(max(x0, x1), x2), W - 1);
+  t.by0 = (int16_t)max(min(min(y0, y1), y2), 0);
+  t.by1 = (int16_t)min(max(max(y0, y1), y2), H - 1);
+  return t;
 }
 
 // Ordered 64-bit visibility key: high word = zRec mapped to an unsigned
@@ -469,15 +504,21 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
 __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Setup& s, const SV& q0, const SV& q1,
                                              const SV& q2, int tex, uint32_t okey, bool from_kept = false) {
   s.r.key = okey | (s.wide ? 0x80000000u : 0u);
-  const int4* src = reinterpret_cast<const int4*>(&s.r);
   int4* dst = reinterpret_cast<int4*>(a.rast + r);
-  dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
   if (s.wide) {
+    dst[0] = make_int4(0, 0, 0, (int)s.r.key);
+    s.w.bx0 = s.r.bx0; s.w.bx1 = s.r.bx1; s.w.by0 = s.r.by0; s.w.by1 = s.r.by1;
     const int4* ws = reinterpret_cast<const int4*>(&s.w);
     int4* wd = reinterpret_cast<int4*>(a.wide + r);
 #pragma unroll
     for (int q = 0; q < 5; ++q) wd[q] = ws[q];
+  } else {  // narrow: |X|, |Y| < 2^14 (setup_tri)
+    dst[0] = make_int4((int)(((uint32_t)(uint16_t)(int16_t)q0.X) | ((uint32_t)(uint16_t)(int16_t)q0.Y << 16)),
+                       (int)(((uint32_t)(uint16_t)(int16_t)q1.X) | ((uint32_t)(uint16_t)(int16_t)q1.Y << 16)),
+                       (int)(((uint32_t)(uint16_t)(int16_t)q2.X) | ((uint32_t)(uint16_t)(int16_t)q2.Y << 16)),
+                       (int)s.r.key);
   }
+  reinterpret_cast<float4*>(dst)[1] = make_float4(s.r.w0, s.r.w1, s.r.w2, s.r.sumf);
   reinterpret_cast<float4*>(a.shade)[r] = make_float4(q0.in, q1.in, q2.in, __int_as_float(tex == -2 && from_kept ? -3 : tex));
   if (tex >= 0) {  // read by the shading only through a texture (rasterizer.go:132-137)
     float4* uv = reinterpret_cast<float4*>(a.suv + r);
@@ -515,7 +556,7 @@ __device__ __forceinline__ void bin_tiles_warp(const FrameArgs& a, uint32_t r, i
   const int ts = 1 << sh;
   const uint32_t lane = threadIdx.x & 31u;
   const DevView& vw = a.views[view];
-  const TriRaster t = a.rast[r];
+  const TriRaster t = unpack_tri(a, r, vw.W, vw.H);
   const uint32_t tx0 = (uint32_t)t.bx0 >> sh, tx1 = (uint32_t)t.bx1 >> sh;
   const uint32_t ty0 = (uint32_t)t.by0 >> sh, ty1 = (uint32_t)t.by1 >> sh;
   const uint32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
@@ -1370,7 +1411,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
       return;
     }
     const uint32_t r = a.rec_of_key[okey];
-    const TriRaster t = a.rast[r];
+    const TriRaster t = unpack_tri(a, r, vw.W, vw.H);
     bool inside;
     float e12f, e20f, al, be, ga;
     edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
@@ -1492,7 +1533,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
         TriRaster t;
         if (valid) {
           r = bin[i];
-          t = a.rast[r];
+          t = unpack_tri(a, r, vw.W, vw.H);
           lx0 = max((int)t.bx0, tx0); lx1 = min((int)t.bx1, tx1);
           ly0 = max((int)t.by0, ty0); ly1 = min((int)t.by1, ty1);
         }
@@ -1586,7 +1627,7 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
           q.flush(skey, a, tx0, ty0);
           if (k + lane < nl) {
             const uint32_t r2 = s_wideq[k + lane];
-            tri[32 + lane] = a.rast[r2];
+            tri[32 + lane] = unpack_tri(a, r2, vw.W, vw.H);
             trec[32 + lane] = r2;
           }
           __syncwarp();

@@ -78,7 +78,7 @@ constexpr Layout make_layout() {
   l.view_tpf_out = o; o += up256(sizeof(unsigned long long));
   l.plan = o; o += up256(sizeof(uint2) * kTiles * kRasterMaxSlices);
   l.empty = o; o += up256(sizeof(uint2) * kTiles);
-  l.rast = o; o += up256(sizeof(TriRaster) * kRecCap);
+  l.rast = o; o += up256(sizeof(TriPacked) * kRecCap);
   l.shade = o; o += up256(sizeof(TriShade) * kRecCap);
   l.suv = o; o += up256(sizeof(TriUV) * kRecCap);
   l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
@@ -294,7 +294,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.items = (const DevItem*)(base + kLayout.items);
   a.texs = (const DevTex*)(base + kLayout.texs);
   a.num_tex = num_textures;
-  a.rast = (TriRaster*)(base + kLayout.rast);
+  a.rast = (TriPacked*)(base + kLayout.rast);
   a.shade = (TriShade*)(base + kLayout.shade);
   a.suv = (TriUV*)(base + kLayout.suv);
   a.wide = (TriWide*)(base + kLayout.wide);
