@@ -128,3 +128,27 @@ def test_back_to_back_async_draws_keep_their_own_tables():
             assert np.array_equal(z.cpu().numpy().view(np.uint32), ref_z.view(np.uint32)), f"view {v}: Z differs"
     finally:
         ctx.close()
+
+
+def test_device_buffers_through_the_c_abi():
+    """gr_device_alloc / gr_copy / gr_device_free: the device memory a host
+    without CUDA of its own uses for batch outputs and parameters."""
+    ctx = gr.Context(0)
+    try:
+        a = np.arange(1000, dtype=np.float32)
+        buf = ctx.device_buffer(a.nbytes).upload(a)
+        assert np.array_equal(buf.download(a.shape, np.float32), a)
+        other = ctx.device_buffer(a.nbytes)
+        R.N.check(R.N.lib().gr_copy(ctx.handle, other.ptr, buf.ptr, a.nbytes))  # device to device
+        assert np.array_equal(other.download(a.shape, np.float32), a)
+        with pytest.raises(ValueError):
+            buf.download((2000,), np.float32)
+        p = R.C.c_void_p()
+        assert R.N.lib().gr_device_alloc(ctx.handle, 0, R.C.byref(p)) == R.N.GR_ERR_INVALID_ARGUMENT
+        assert R.N.lib().gr_copy(ctx.handle, None, buf.ptr, 4) == R.N.GR_ERR_INVALID_ARGUMENT
+        assert R.N.lib().gr_copy(ctx.handle, None, None, 0) == R.N.GR_OK
+        buf.free()
+        other.free()
+        assert R.N.lib().gr_device_free(ctx.handle, None) == R.N.GR_OK
+    finally:
+        ctx.close()
