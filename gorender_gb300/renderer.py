@@ -129,6 +129,13 @@ class DeviceBuffer:
         N.check(N.lib().gr_copy(self.ctx.handle, out.ctypes.data, self.ptr, out.nbytes))
         return out
 
+    @staticmethod
+    def download_from(ctx: "Context", ptr: int, shape, dtype) -> np.ndarray:
+        """A host copy of device memory at ptr (any device pointer of ctx's GPU)."""
+        out = np.empty(shape, dtype)
+        N.check(N.lib().gr_copy(ctx.handle, out.ctypes.data, int(ptr), out.nbytes))
+        return out
+
     def free(self):
         if self._p and self._p.value and self.ctx.handle:
             N.check(N.lib().gr_device_free(self.ctx.handle, self._p))

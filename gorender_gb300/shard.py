@@ -108,3 +108,62 @@ class ShardedBatch:
             rgba.free()
             z.free()
         self.outputs = []
+
+
+def allreduce_host(dist):
+    """A sum over ranks of host arrays, in place, through a torch.distributed
+    process group (gloo or any backend that takes CPU tensors)."""
+    import torch
+
+    def reduce(arrays):
+        for a in arrays:
+            t = torch.from_numpy(a)
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return reduce
+
+
+class ShardedDiff:
+    """The differentiable forward and backward of one mesh over many views,
+    the views dealt across ranks (one process per GPU).
+
+    The loss is a sum over views and pixels, so it and every gradient (vertex
+    positions and colours, texels, the light) are sums of the ranks' shares:
+    each rank differentiates its own views and one sum over ranks of its
+    loss and gradients gives the whole step's -- the only data that crosses
+    between GPUs (16 + 12 bytes a vertex, 16 a texel, 32 for the light and
+    the loss).  ``views`` is the full list of ``renderer.diff_views``;
+    ``indices`` this rank's share (``partition_views`` of equal costs).
+    Parameters and targets are device buffers of the rank's context; the
+    target holds the pixels of this rank's views only, in their order."""
+
+    def __init__(self, ctx: R.Context, mesh: int, world, views, indices: Sequence[int],
+                 tex_size: Tuple[int, int] = (0, 0)):
+        self.ctx = ctx
+        self.indices = list(indices)
+        self.views = [views[i] for i in self.indices]
+        self.pixels = sum(w * h for w, h, _, _, _ in self.views)
+        self.diff = R.Diff(ctx, mesh, world, self.views, tex_size=tex_size) if self.views else None
+
+    def forward(self, pos, vcol, tex, light, target, image=None) -> float:
+        """This rank's share of the loss (device pointers as in Diff.forward)."""
+        return self.diff.forward(pos, vcol, tex, light, target, image) if self.diff else 0.0
+
+    def step(self, pos, vcol, tex, light, target, grads, shapes, allreduce):
+        """Forward + backward of this rank's views, then the sum over ranks:
+        returns (loss, light gradient, [position, colour, texel gradients])
+        of the whole step as host arrays; ``grads`` are this rank's device
+        gradient buffers and ``shapes`` their (shape, dtype)."""
+        loss = np.array([self.forward(pos, vcol, tex, light, target)], np.float64)
+        if self.diff:
+            g_light = np.asarray(self.diff.backward(*(int(g) for g in grads)), np.float64).reshape(3)
+            host = [R.DeviceBuffer.download_from(self.ctx, g, shape, dtype) for g, (shape, dtype) in zip(grads, shapes)]
+        else:
+            g_light = np.zeros(3, np.float64)
+            host = [np.zeros(shape, dtype) for shape, dtype in shapes]
+        allreduce([loss, g_light] + host)
+        return float(loss[0]), g_light, host
+
+    def close(self):
+        if self.diff:
+            self.diff.close()
+            self.diff = None
