@@ -114,6 +114,7 @@ struct gr_context {
   uint32_t* bins = nullptr;
   uint32_t* bin_count = nullptr;
   uint32_t* tile_cost = nullptr;    // per tile: boxes of its large entries (k_plan's cost estimate)
+  uint4* tile_info = nullptr;       // per tile: entries, slices, key slot (k_plan)
   uint32_t bin_cap = 0;
   uint32_t tiles_cap = 0;
   uint2* big = nullptr;             // multi-tile queue: (record, view)
@@ -146,6 +147,7 @@ struct gr_context {
   uint32_t* ovl_key = nullptr;      // per pixel of all views (zero when idle)
   unsigned long long* pkey = nullptr;  // per pixel of all views: keys for k_resolve
   uint64_t pkey_pixels = 0;
+  unsigned long long* slot_keys = nullptr;  // keys of split tiles' slices, 4 x pkey_pixels
   uint64_t ovl_pixels = 0;
   int raster_waves = 1;             // persistent raster CTAs = SMs x resident CTAs x waves
   int last_views = 0;               // views of the last batched draw
@@ -296,10 +298,10 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
     if ((st = sync())) return st;
     uint32_t nt = std::max(tiles, c->tiles_cap);
     uint32_t nc = std::max(want_bin, c->bin_cap);
-    dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost);
+    dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->tile_info);
     c->tiles_cap = 0; c->bin_cap = 0;
     if ((st = dev_alloc(&c->bins, (size_t)nt * nc)) || (st = dev_alloc(&c->bin_count, nt)) ||
-        (st = dev_alloc(&c->tile_cost, nt)))
+        (st = dev_alloc(&c->tile_cost, nt)) || (st = dev_alloc(&c->tile_info, nt)))
       return st;
     CK(cudaMemsetAsync(c->bin_count, 0, sizeof(uint32_t) * nt, c->stream));
     CK(cudaMemsetAsync(c->tile_cost, 0, sizeof(uint32_t) * nt, c->stream));
@@ -461,8 +463,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   if (separate && total_pixels > c->pkey_pixels) {
     CK(cudaStreamSynchronize(c->stream));
     dev_free(c->pkey);
+    dev_free(c->slot_keys);
     c->pkey_pixels = 0;
-    if ((st = dev_alloc(&c->pkey, (size_t)total_pixels))) return st;
+    if ((st = dev_alloc(&c->pkey, (size_t)total_pixels)) || (st = dev_alloc(&c->slot_keys, 4 * (size_t)total_pixels)))
+      return st;
     c->pkey_pixels = total_pixels;
   }
   const int slot = (c->stage_slot + 1) % kStageSlots;
@@ -644,6 +648,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.ovl_cap = c->ovl_cap;
   a.ovl_key = c->ovl_key;
   a.pkey = separate ? c->pkey : nullptr;
+  a.tile_info = c->tile_info;
+  a.slot_keys = separate ? c->slot_keys : nullptr;
+  a.slot_cap = separate ? (uint32_t)std::min<uint64_t>((4 * c->pkey_pixels) >> (2 * c->tile_shift), 0xFFFFFFF0u) : 0u;
   // Many views shaded in place: tiles without bin entries (most of a batch
   // of small meshes) are cleared by k_clear beside the raster (a 256-view
   // batch 1.81 -> 1.62 ms); one view keeps them in the raster queue, where
@@ -715,13 +722,13 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
 // signature no longer matches must be captured again before it runs.
 uint64_t buffers_signature(const gr_context* c) {
   const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->suv, (uintptr_t)c->wide, (uintptr_t)c->tcol,
-                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->gkey,
+                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->tile_info, (uintptr_t)c->gkey,
                           (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->kept, c->kept_cap, (uintptr_t)c->big, (uintptr_t)c->vlight,
                           (uintptr_t)c->vclip, (uintptr_t)c->vscr,
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
                           (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, (uintptr_t)c->empty_tiles, c->empty_cap, c->rec_cap, c->key_cap, c->bin_cap,
                           c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_cost,
-                          (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key, (uintptr_t)c->pkey,
+                          (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key, (uintptr_t)c->pkey, (uintptr_t)c->slot_keys,
                           c->ovl_cap};
   uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
   for (uintptr_t v : ps) {
@@ -873,11 +880,12 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->d_texs); dev_free(c->d_tables);
   if (c->h_tables) cudaFreeHost(c->h_tables);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->suv); dev_free(c->wide); dev_free(c->tcol);
-  dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->big);
+  dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->tile_info);
+  dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->kept); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);
   dev_free(c->view_tpf); dev_free(c->view_tpf_out); dev_free(c->plan); dev_free(c->empty_tiles);
-  dev_free(c->ovl); dev_free(c->ovl_key); dev_free(c->pkey);
+  dev_free(c->ovl); dev_free(c->ovl_key); dev_free(c->pkey); dev_free(c->slot_keys);
   if (c->h_view_tpf) cudaFreeHost(c->h_view_tpf);
   dev_free(c->work); dev_free(c->d_result);
   if (c->h_result) cudaFreeHost(c->h_result);

@@ -240,6 +240,11 @@ struct FrameArgs {
   uint32_t* ovl_key;                // per pixel of every view: max (order key * 2 + vertex mark), 0 = none
   unsigned long long* pkey;         // per pixel of every view: final visibility keys, shaded by k_resolve
                                     // (null: k_raster shades each tile itself)
+  uint4* tile_info;                 // per tile, from k_plan: x bin entries, y raster slices, z first key
+                                    // slot of a split tile of a one-view frame (kNoSlot: merged in gkey)
+  unsigned long long* slot_keys;    // one-view frames: slot_cap slots of TS x TS keys, one per slice of a
+                                    // split tile; k_resolve takes the max over a tile's slots
+  uint32_t slot_cap;
   unsigned long long total_pixels;  // sum of the views' pixels
 };
 
@@ -247,6 +252,7 @@ struct FrameArgs {
 // winning face's global index (or kNoFace) into out_rgba instead of a colour,
 // computed from the visibility key alone, and writes no depth.
 constexpr uint32_t kViewFaceIds = 0x80000000u;
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;  // TileInfo: a split tile merged through gkey
 constexpr uint32_t kNoFace = 0xFFFFFFFFu;
 
 // ---- differentiable shading (an extension with no counterpart in the reference) ----

@@ -1482,9 +1482,9 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
   const int warp = tid >> 5;
   const DevView& vw = a.views[view];
   // A tile's bin is split into up to kRasterMaxSlices slices, one work item each.
-  const uint32_t count = a.bin_count[tile];
-  const uint32_t n = min(count, a.bin_cap);
-  const uint32_t nslices = tile_slices(a, n, count * (uint32_t)kEntryCost + a.tile_cost[tile]);
+  const uint4 ti = a.tile_info[tile];  // k_plan: entries, slices, key slot
+  const uint32_t n = ti.x;
+  const uint32_t nslices = ti.y;
   if (slice >= nslices) return;
   const uint32_t per = (((n + nslices - 1) / nslices) + 31u) & ~31u;
   const uint32_t lo = min(n, slice * per), hi = min(n, lo + per);
@@ -1648,6 +1648,16 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
       __syncthreads();
     }
 
+    if (nslices > 1 && ti.z != kNoSlot) {
+      // One view: this slice's keys go to a slot of their own with plain
+      // stores, and k_resolve takes the max over the tile's slots -- the
+      // kernel boundary orders them, so no slice waits on a fence or hands
+      // over (the merge below took a fifth of this kernel's warp time on
+      // single frames).
+      unsigned long long* dst = a.slot_keys + (size_t)(ti.z + slice) * (TS * TS);
+      for (int i = tid; i < TS * TS; i += kThreads) dst[i] = skey[(i / TS) * kStride + (i % TS)];
+      return;
+    }
     if (nslices > 1) {
       // Merge this slice's keys into the tile's global keys; the last slice to
       // arrive resolves the tile and returns the global keys to zero (zero is
@@ -1715,10 +1725,6 @@ __device__ __forceinline__ void raster_item(const FrameArgs& a, uint32_t tile, u
         }
       }
     }
-  }
-  if (tid == 0) {  // ready for the next frame
-    a.bin_count[tile] = 0u;
-    a.tile_cost[tile] = 0u;
   }
 }
 
@@ -1823,6 +1829,10 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   const uint32_t count = valid ? a.bin_count[tile] : 0u;
   const uint32_t cost = valid ? count * (uint32_t)kEntryCost + a.tile_cost[tile] : 0u;
   const uint32_t ns = valid ? tile_slices(a, min(count, a.bin_cap), cost) : 0u;
+  if (valid) {  // the bins are complete: ready for the next frame's appends
+    a.bin_count[tile] = 0u;
+    a.tile_cost[tile] = 0u;
+  }
   // the tile's view (last view whose first tile <= tile), packed into the
   // work item beside the slice so the raster CTAs do not search for it
   int view = 0;
@@ -1856,6 +1866,15 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   }
   __syncthreads();
   if (!valid) return;
+  // A split tile of a one-view frame into at most 8 slices: its slices' keys
+  // in the slots of its plan items (the front of the queue), while they fit.
+  // k_resolve then reads a key per slice for each of the tile's pixels;
+  // beyond 8 slices that cost more than the merge (same-box A/B: heightfield
+  // 0.1227 -> 0.1183 ms with the cap, the 5 M-face frame unchanged; without
+  // it the latter 1 % slower).
+  const uint32_t slot =
+      heavy && ns > 1 && ns <= 8u && a.slot_keys && s_bf + mf + ns <= a.slot_cap ? s_bf + mf : kNoSlot;
+  a.tile_info[tile] = make_uint4(min(count, a.bin_cap), ns, slot, 0u);
   if (clear) {
     if (s_be + me < a.empty_cap) a.empty_tiles[s_be + me] = make_uint2(tile, (uint32_t)view);
   } else if (heavy) {
@@ -1955,9 +1974,19 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
   const DevView& vw = a.views[v];
   const uint32_t o = (uint32_t)(p - vw.pix_base);
   const int y = (int)(o / (uint32_t)vw.W), x = (int)(o - (uint32_t)y * (uint32_t)vw.W);
+  unsigned long long k;
+  const int sh = a.tile_shift, ts = 1 << sh;
+  const uint4 ti = a.tile_info[vw.tile_base + (uint32_t)(y >> sh) * (uint32_t)vw.tiles_x + (uint32_t)(x >> sh)];
+  if (ti.y > 1 && ti.z != kNoSlot) {  // a split tile: the max over its slices' slots
+    const unsigned long long* sk = a.slot_keys + (size_t)ti.z * (size_t)(ts * ts) + (size_t)((y & (ts - 1)) * ts + (x & (ts - 1)));
+    k = sk[0];
+    for (uint32_t s = 1; s < ti.y; ++s) k = max(k, sk[(size_t)s * (size_t)(ts * ts)]);
+  } else {
+    k = a.pkey[p];
+  }
   uint32_t c;
   float z;
-  resolve_pixel(a, vw, x, y, a.pkey[p], c, z);
+  resolve_pixel(a, vw, x, y, k, c, z);
   vw.out_rgba[o] = c;
   if (!(vw.flags & kViewFaceIds)) vw.out_z[o] = z;  // face-id views output no depth
 }

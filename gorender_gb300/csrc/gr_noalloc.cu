@@ -65,7 +65,7 @@ constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 // Byte offsets of the sub-buffers inside g_scratch.
 struct Layout {
   size_t items, texs, views, view_tpf, view_tpf_out, plan, empty, rast, shade, suv, wide, tcol, keys, bins, bin_count, tile_cost, big, clip, kept,
-      vlight, vclip, vscr, gkey, tile_done, work, result, check, end;
+      vlight, vclip, vscr, gkey, tile_done, tile_info, work, result, check, end;
 };
 
 constexpr Layout make_layout() {
@@ -95,6 +95,7 @@ constexpr Layout make_layout() {
   l.vscr = o; o += up256(sizeof(float2) * kMaxVertices);
   l.gkey = o; o += up256(sizeof(unsigned long long) * kTiles * 1024);
   l.tile_done = o; o += up256(sizeof(uint32_t) * kTiles);
+  l.tile_info = o; o += up256(sizeof(uint4) * kTiles);
   l.work = o; o += up256(sizeof(DevWork));
   l.result = o; o += up256(sizeof(DevResult));
   l.check = o; o += up256(sizeof(uint32_t));
@@ -314,6 +315,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.vert_blocks = vert_blocks;
   a.gkey = (unsigned long long*)(base + kLayout.gkey);
   a.tile_done = (uint32_t*)(base + kLayout.tile_done);
+  a.tile_info = (uint4*)(base + kLayout.tile_info);
   a.work = (DevWork*)(base + kLayout.work);
   a.result = (DevResult*)(base + kLayout.result);
   a.view_tpf = (unsigned long long*)(base + kLayout.view_tpf);
