@@ -129,7 +129,7 @@ struct gr_context {
   float* vlight = nullptr;          // per-normal Gouraud intensities
   uint64_t vlight_cap = 0;
   float4* vclip = nullptr;          // per item vertex: clip position and screen x, y (k_vertex)
-  float2* vscr = nullptr;
+  float4* vscr = nullptr;
   uint64_t vert_cap = 0;
   unsigned long long* view_tpf = nullptr;
   unsigned long long* view_tpf_out = nullptr;
@@ -631,7 +631,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.clip_cap = c->clip_cap;
   a.kept = c->kept;
   a.kept_cap = c->kept_cap;
-  a.setup_blocks = (int)std::min<uint64_t>(kSetupBlocks, (faces + kProjectThreads - 1) / kProjectThreads);
+  a.setup_blocks = (int)std::min<uint64_t>(setup_blocks_max(project_g), (faces + kProjectThreads - 1) / kProjectThreads);
   a.vlight = c->vlight;
   a.light_blocks = light_blocks;
   a.vclip = c->vclip;

@@ -27,8 +27,14 @@ static_assert(kRasterMaxSlices <= 32, "a raster work item packs its slice into 5
 constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a tile is split
 constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
-constexpr int kSetupCtasPerSm = 2;            // k_setup: resident CTAs an SM (128 registers a thread)
-constexpr int kSetupBlocks = kSetupCtasPerSm * 152;  // k_setup grid (grid-stride over the kept faces)
+// k_setup: resident CTAs an SM by the frame's face count (its k_cull lane
+// count): 2 (up to 128 registers a thread, no spills) below 1 M faces; 3 (up to
+// 85 registers, a few bytes spilled) from 1 M faces on, where more warps hide
+// more of the gathers (same-box A/B: the 256-view batch 40 us faster, the
+// 5 M-face frame 3 us; the 200k-face frame 1.5 us slower with 3)
+__host__ __device__ constexpr int setup_ctas_per_sm(int project_g) { return project_g >= 2 ? 3 : 2; }
+// k_setup grid (grid-stride over the kept faces)
+__host__ __device__ constexpr int setup_blocks_max(int project_g) { return setup_ctas_per_sm(project_g) * 152; }
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 constexpr int kBigBlocks = 3 * 152;           // k_bin_big / k_overlay grid (grid-stride over the queue)
 constexpr int kClearBlocks = 8 * 152;         // k_clear grid (grid-stride over the empty tiles)
@@ -217,7 +223,7 @@ struct FrameArgs {
   float* vlight;                    // per-normal Gouraud intensities (k_light)
   int light_blocks;                 // k_light grid (0: no Gouraud item)
   float4* vclip;                    // per item vertex: clip-space position (k_vertex)
-  float2* vscr;                     // per item vertex: screen x, y before int() (k_vertex)
+  float4* vscr;                     // per item vertex: screen x, y before int() and clip W (k_vertex)
   int vert_blocks;                  // k_vertex grid
   unsigned long long* gkey;         // tiles x 1024 merged visibility keys of split tiles (zero when idle)
   uint32_t* tile_done;              // per tile: slices finished (zero when idle)

@@ -616,7 +616,8 @@ __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
     if (v < it.nv) {
       const V4 c = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)v));
       a.vclip[it.vert_base + v] = make_float4(c.x, c.y, c.z, c.w);
-      a.vscr[it.vert_base + v] = screen_of(c, s_S);
+      const float2 sc = screen_of(c, s_S);
+      a.vscr[it.vert_base + v] = make_float4(sc.x, sc.y, c.w, 0.0f);  // W beside x, y: one gather in k_setup
     }
   }
 }
@@ -776,9 +777,10 @@ __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
 // screen vertices, the bin test (TPF), setup, the record and its bins.  A
 // warp's faces may belong to different items and views.
 // ---------------------------------------------------------------------------
-// 2 CTAs per SM (up to 128 registers a thread, no spills): measured 3 us
-// less than 4 CTAs with spills on a 200k-face frame, 24 us less on 3.6 M faces.
-__global__ void __launch_bounds__(kProjectThreads, kSetupCtasPerSm) k_setup(const FrameArgs a) {
+// CTAS resident CTAs an SM (setup_ctas_per_sm): 2 measured 3 us less than 4
+// CTAs with spills on a 200k-face frame.
+template <int CTAS>
+__global__ void __launch_bounds__(kProjectThreads, CTAS) k_setup(const FrameArgs a) {
   griddep_wait();
   const uint32_t nkept = min(*(volatile uint32_t*)&a.work->nkept, a.kept_cap);
   const unsigned lane = lane_id();
@@ -808,9 +810,10 @@ __global__ void __launch_bounds__(kProjectThreads, kSetupCtasPerSm) k_setup(cons
       const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
       const uint32_t v0 = vbase + i0, v1 = vbase + i1, v2 = vbase + i2;
       face_attributes(a, it, f, i0, i1, i2, it.world, p0, p1, p2, tex);
-      s0 = sv_of(__ldg(a.vscr + v0), __ldg(&a.vclip[v0].w), p0);
-      s1 = sv_of(__ldg(a.vscr + v1), __ldg(&a.vclip[v1].w), p1);
-      s2 = sv_of(__ldg(a.vscr + v2), __ldg(&a.vclip[v2].w), p2);
+      const float4 q0 = __ldg(a.vscr + v0), q1 = __ldg(a.vscr + v1), q2 = __ldg(a.vscr + v2);
+      s0 = sv_of(make_float2(q0.x, q0.y), q0.z, p0);
+      s1 = sv_of(make_float2(q1.x, q1.y), q1.z, p1);
+      s2 = sv_of(make_float2(q2.x, q2.y), q2.z, p2);
       if (bin_test(s0, s1, s2, (float)W, (float)H)) {
         ntpf = 1;
         // ShowFaces off: triangles still count in TPF but are not rasterised (renderer.go:180)
@@ -1894,9 +1897,11 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
   __shared__ int s_view;
   const uint32_t front = *(volatile uint32_t*)&a.work->plan_front;
   const uint32_t total = front + *(volatile uint32_t*)&a.work->plan_back;
-  for (;;) {
+  // The first item of every CTA is its block index; later ones come from the
+  // counter, past the grid (no burst of atomics on one address at the start).
+  for (bool first = true;; first = false) {
     if (threadIdx.x == 0) {
-      const uint32_t i = atomicAdd(&a.work->raster_next, 1u);
+      const uint32_t i = first ? blockIdx.x : gridDim.x + atomicAdd(&a.work->raster_next, 1u);
       s_item = i;
       if (i < total) {
         const uint2 w = i < front ? a.plan[i] : a.plan[a.plan_cap - 1u - (i - front)];
@@ -2129,7 +2134,8 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
       k_clip<<<kClipBlocks, 128, 0, s2>>>(a);
       ++n;
     }
-    launch_after(k_setup, a.setup_blocks, kProjectThreads, s, a);
+    if (setup_ctas_per_sm(a.project_g) == 3) launch_after(k_setup<3>, a.setup_blocks, kProjectThreads, s, a);
+    else launch_after(k_setup<2>, a.setup_blocks, kProjectThreads, s, a);
     ++n;
     if (events) cudaEventRecord((cudaEvent_t)events[1], s);
     if (events) k_bin_big<<<big_blocks, 256, 0, s>>>(a);  // timed stages: plain launches

@@ -92,7 +92,7 @@ constexpr Layout make_layout() {
   l.kept = o; o += up256(sizeof(uint2) * kMaxFaces);
   l.vlight = o; o += up256(sizeof(float) * kMaxNormals);
   l.vclip = o; o += up256(sizeof(float4) * kMaxVertices);
-  l.vscr = o; o += up256(sizeof(float2) * kMaxVertices);
+  l.vscr = o; o += up256(sizeof(float4) * kMaxVertices);
   l.gkey = o; o += up256(sizeof(unsigned long long) * kTiles * 1024);
   l.tile_done = o; o += up256(sizeof(uint32_t) * kTiles);
   l.tile_info = o; o += up256(sizeof(uint4) * kTiles);
@@ -308,10 +308,10 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.clip = (uint2*)(base + kLayout.clip);
   a.kept = (uint2*)(base + kLayout.kept);
   a.kept_cap = kMaxFaces;
-  a.setup_blocks = (int)std::min<long>(kSetupBlocks, (faces + kProjectThreads - 1) / kProjectThreads);
+  a.setup_blocks = (int)std::min<long>(setup_blocks_max(a.project_g), (faces + kProjectThreads - 1) / kProjectThreads);
   a.vlight = (float*)(base + kLayout.vlight);
   a.vclip = (float4*)(base + kLayout.vclip);
-  a.vscr = (float2*)(base + kLayout.vscr);
+  a.vscr = (float4*)(base + kLayout.vscr);
   a.vert_blocks = vert_blocks;
   a.gkey = (unsigned long long*)(base + kLayout.gkey);
   a.tile_done = (uint32_t*)(base + kLayout.tile_done);
