@@ -531,6 +531,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     std::memcpy(d.mvp, items[i].mvp, sizeof(d.mvp));
     std::memcpy(d.world, items[i].world, sizeof(d.world));
     std::memcpy(d.bbox, mr.bbox, sizeof(d.bbox));
+    d.vis = box_visibility(d.mvp, d.bbox);
     d.pos = mr.pos; d.vnrm = mr.vnrm; d.fnrm = mr.fnrm; d.vidx = mr.vidx; d.nidx = mr.nidx;
     d.uv = mr.uv; d.tex = mr.tex; d.vcol = mr.vcol;
     d.nv = mr.nv; d.nn = mr.nn; d.nf = mr.nf;

@@ -154,6 +154,8 @@ __global__ void __launch_bounds__(1024) k_diff_bbox(const float* __restrict__ po
   }
   __syncthreads();
   for (int i = tid; i < num_items * 32; i += blockDim.x) items[i / 32].bbox[i % 32] = s_b[i % 32];
+  // and each view's BoxVisibility of this box, which k_cull reads
+  for (int i = tid; i < num_items; i += blockDim.x) items[i].vis = box_visibility(items[i].mvp, s_b);
 }
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }

@@ -88,7 +88,41 @@ struct DevItem {
   int view;                         // index into FrameArgs::views
   uint32_t vert_base;               // first entry of this item in FrameArgs::vclip / vscr
   int vert_block_base;              // first k_vertex block of this item
+  int vis;                          // Frustum.BoxVisibility of bbox under mvp (box_visibility)
 };
+
+// Frustum.BoxVisibility (clipping.go:131-154) of a transformed bounding box
+// (renderer.go:268-275): 0 outside, 1 intersecting, 2 inside.  bbox holds the
+// 8 corners x 4 of Mesh.BoundingBox; each corner is transformed as
+// matrixMultiplyVec4 does, ((m0 x + m1 y) + m2 z) + m3 w, and tested against
+// the six planes (zNear = 0, zFar = 50) with DistanceToVertex = N.v - N.P.
+// Plain float operations, one rounding each: device code is built with
+// --fmad=false and host code with -ffp-contract=off, so host and device give
+// the same bits.
+__host__ __device__ inline int box_visibility(const float* m, const float* bbox) {
+  const float P[6][4] = {{-1, 0, 0, 1}, {1, 0, 0, 1}, {0, -1, 0, 1}, {0, 1, 0, 1}, {0, 0, 0, 1}, {0, 0, 50, 1}};
+  const float N[6][4] = {{1, 0, 0, 1}, {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}, {0, 0, -1, 0}, {0, 0, 1, 0}};
+  unsigned out[8];
+  for (int c = 0; c < 8; ++c) {
+    const float* b = bbox + 4 * c;
+    float v[4];
+    for (int r = 0; r < 4; ++r) v[r] = ((m[4 * r] * b[0] + m[4 * r + 1] * b[1]) + m[4 * r + 2] * b[2]) + m[4 * r + 3] * b[3];
+    unsigned bits = 0;
+    for (int i = 0; i < 6; ++i) {
+      const float nv = ((N[i][0] * v[0] + N[i][1] * v[1]) + N[i][2] * v[2]) + N[i][3] * v[3];
+      const float np = ((N[i][0] * P[i][0] + N[i][1] * P[i][1]) + N[i][2] * P[i][2]) + N[i][3] * P[i][3];
+      if (nv - np > 0.0f) bits |= 1u << i;
+    }
+    out[c] = bits;
+  }
+  for (int i = 0; i < 6; ++i) {
+    int outside = 0;
+    for (int c = 0; c < 8; ++c) outside += (out[c] >> i) & 1u;
+    if (outside == 8) return 0;
+    if (outside > 0) return 1;
+  }
+  return 2;
+}
 
 // Raster setup of one binned triangle (64 bytes, in registers and shared
 // memory; stored as a TriPacked).  For "narrow" triangles

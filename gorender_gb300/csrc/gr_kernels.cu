@@ -657,10 +657,7 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 template <int G>
 __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
   griddep_wait();
-  __shared__ float s_mvp[16];
   __shared__ int s_item;
-  __shared__ int s_vis;
-  __shared__ unsigned s_out[8];
   constexpr int kWarps = kProjectThreads / 32;
   __shared__ uint32_t s_wn[kWarps];
   __shared__ uint32_t s_base;
@@ -671,33 +668,11 @@ __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
   __syncthreads();
   const int item = s_item;
   const DevItem& it = a.items[item];
-  const DevView& vw = a.views[it.view];
-  if (tid < 16) s_mvp[tid] = it.mvp[tid];
-  __syncthreads();
-  // Frustum.BoxVisibility of the transformed bounding box (renderer.go:268-275).
-  if (tid < 8) {
-    V4 c = mat_vec(s_mvp, V4{it.bbox[4 * tid], it.bbox[4 * tid + 1], it.bbox[4 * tid + 2], it.bbox[4 * tid + 3]});
-    unsigned bits = 0;
-    for (int i = 0; i < 6; ++i) {
-      float d = fs(dot4(plane_n(i), c), dot4(plane_n(i), plane_p(i)));  // DistanceToVertex
-      if (d > 0.0f) bits |= 1u << i;
-    }
-    s_out[tid] = bits;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int vis = 2;  // Inside
-    for (int i = 0; i < 6; ++i) {
-      int outside = 0;
-      for (int k = 0; k < 8; ++k) outside += (s_out[k] >> i) & 1u;
-      if (outside == 8) { vis = 0; break; }
-      if (outside > 0) { vis = 1; break; }
-    }
-    s_vis = vis;
-  }
-  __syncthreads();
-  const int vis = s_vis;
+  // Frustum.BoxVisibility of the transformed bounding box (renderer.go:268-275),
+  // computed once per item where the box is known (box_visibility)
+  const int vis = it.vis;
   if (vis == 0) return;  // whole block: object outside the frustum
+  const DevView& vw = a.views[it.view];
 
   const uint32_t fl = vw.flags;
   const unsigned lane = lane_id();

@@ -220,6 +220,7 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
     std::memcpy(d.mvp, objects[i].mvp, sizeof(d.mvp));
     std::memcpy(d.world, objects[i].world, sizeof(d.world));
     std::memcpy(d.bbox, objects[i].bbox, sizeof(d.bbox));
+    d.vis = box_visibility(d.mvp, d.bbox);
     d.pos = m.positions; d.vnrm = m.vertex_normals; d.fnrm = m.face_normals; d.vidx = m.vertex_indices;
     d.nidx = m.normal_indices; d.uv = m.uvs; d.tex = m.face_textures; d.vcol = m.vertex_colors;
     d.nv = m.num_vertices; d.nn = m.vertex_normals ? m.num_normals : 0; d.nf = m.num_faces;
