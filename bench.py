@@ -147,7 +147,7 @@ def algorithmic_bytes(scene):
 # replay runs it beside k_setup and k_bin_big).
 STAGES = {"project_stage": "k_light + k_vertex + k_cull + k_clip + k_setup",
           "bin_stage": "k_bin_big (+ k_overlay)",
-          "raster_stage": "k_plan + k_raster + k_resolve (one view) or k_plan + k_clear + k_raster (a batch)"}
+          "raster_stage": "k_plan + k_raster + k_resolve (one view) or k_plan + k_raster, which also clears the empty tiles (a batch)"}
 STAGE_KERNELS = {"project_stage": ["k_light", "k_vertex", "k_cull", "k_clip", "k_setup"],
                  "bin_stage": ["k_bin_big", "k_overlay"],
                  "raster_stage": ["k_plan", "k_raster", "k_resolve", "k_clear"],

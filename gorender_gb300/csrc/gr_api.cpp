@@ -109,8 +109,8 @@ struct gr_context {
   TriWide* wide = nullptr;
   TriColor* tcol = nullptr;
   uint32_t rec_cap = 0;
-  uint32_t* rec_of_key = nullptr;
-  uint32_t key_cap = 0;
+  uint32_t* rec_of_face = nullptr;  // per face of the frame: its record, or its clip slot
+  uint32_t face_cap = 0;
   uint32_t* bins = nullptr;
   uint32_t* bin_count = nullptr;
   uint32_t* tile_cost = nullptr;    // per tile: boxes of its large entries (k_plan's cost estimate)
@@ -136,7 +136,7 @@ struct gr_context {
   unsigned long long* h_view_tpf = nullptr;
   int views_cap = 0;
   uint2* plan = nullptr;            // raster work queue
-  uint2* empty_tiles = nullptr;     // tiles without bin entries (k_clear)
+  uint2* empty_tiles = nullptr;     // tiles without bin entries (cleared by k_raster<TS, true>)
   uint32_t empty_cap = 0;
   uint32_t plan_cap = 0;
   bool fog_on = false;              // FrameBuffer.Fog fused into every frame
@@ -284,13 +284,13 @@ int32_t ensure_frame_buffers(gr_context* c, uint64_t faces, uint32_t tiles) {
       return st;
     c->rec_cap = (uint32_t)want_rec;
   }
-  uint64_t want_key = (uint64_t)kKeysPerFace * faces + kKeysPerFace;
-  if (want_key > c->key_cap) {
+  if (faces > c->face_cap) {
     if ((st = sync())) return st;
-    dev_free(c->rec_of_key);
-    c->key_cap = 0;
-    if ((st = dev_alloc(&c->rec_of_key, want_key))) return st;
-    c->key_cap = (uint32_t)want_key;
+    dev_free(c->rec_of_face);
+    c->face_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(faces, 1024);
+    if ((st = dev_alloc(&c->rec_of_face, cap))) return st;
+    c->face_cap = (uint32_t)cap;
   }
   uint32_t want_bin = c->want_bin_cap;
   if (want_bin == 0) want_bin = std::max<uint32_t>(1024, next_pow2(4 * (2 * faces) / std::max<uint32_t>(tiles, 1)));
@@ -611,7 +611,6 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.bin_cap = c->bin_cap;
   a.rec_cap = c->rec_cap;
   a.big_cap = c->big_cap;
-  a.key_cap = c->key_cap;
   a.items = ditems;
   a.texs = c->d_texs;
   a.num_tex = (int)c->texs.size();
@@ -620,7 +619,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.suv = c->suv;
   a.wide = c->wide;
   a.tcol = c->tcol;
-  a.rec_of_key = c->rec_of_key;
+  a.rec_of_face = c->rec_of_face;
+  a.face_cap = c->face_cap;
   a.bins = c->bins;
   a.bin_count = c->bin_count;
   a.tile_cost = c->tile_cost;
@@ -653,9 +653,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   a.slot_keys = separate ? c->slot_keys : nullptr;
   a.slot_cap = separate ? (uint32_t)std::min<uint64_t>((4 * c->pkey_pixels) >> (2 * c->tile_shift), 0xFFFFFFF0u) : 0u;
   // Many views shaded in place: tiles without bin entries (most of a batch
-  // of small meshes) are cleared by k_clear beside the raster (a 256-view
-  // batch 1.81 -> 1.62 ms); one view keeps them in the raster queue, where
-  // they cost less than k_clear's launch (0.153 against 0.166 ms a frame).
+  // of small meshes) are cleared by the raster CTAs once their queue is
+  // empty, without keys (a 256-view batch 1.81 -> 1.62 ms with a kernel of
+  // their own, 1.335 -> 1.286 ms inside k_raster); one view keeps them in the
+  // raster queue (0.153 against 0.166 ms a frame with the separate kernel).
   a.clear_empty = (!separate && nviews > 1) ? 1 : 0;
   if (a.clear_empty && total_tiles > c->empty_cap) {  // allocated only for such frames
     CK(cudaStreamSynchronize(c->stream));
@@ -723,11 +724,11 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
 // signature no longer matches must be captured again before it runs.
 uint64_t buffers_signature(const gr_context* c) {
   const uintptr_t ps[] = {(uintptr_t)c->rast, (uintptr_t)c->shade, (uintptr_t)c->suv, (uintptr_t)c->wide, (uintptr_t)c->tcol,
-                          (uintptr_t)c->rec_of_key, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->tile_info, (uintptr_t)c->gkey,
+                          (uintptr_t)c->rec_of_face, (uintptr_t)c->bins, (uintptr_t)c->bin_count, (uintptr_t)c->tile_cost, (uintptr_t)c->tile_info, (uintptr_t)c->gkey,
                           (uintptr_t)c->tile_done, (uintptr_t)c->clip, (uintptr_t)c->kept, c->kept_cap, (uintptr_t)c->big, (uintptr_t)c->vlight,
                           (uintptr_t)c->vclip, (uintptr_t)c->vscr,
                           (uintptr_t)c->d_texs, (uintptr_t)c->view_tpf, (uintptr_t)c->view_tpf_out,
-                          (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, (uintptr_t)c->empty_tiles, c->empty_cap, c->rec_cap, c->key_cap, c->bin_cap,
+                          (uintptr_t)c->h_view_tpf, (uintptr_t)c->plan, (uintptr_t)c->empty_tiles, c->empty_cap, c->rec_cap, c->face_cap, c->bin_cap,
                           c->big_cap, c->clip_cap, c->plan_cap, (uintptr_t)c->tile_shift, c->slice_cost,
                           (uintptr_t)c->raster_waves, c->texs.size(), (uintptr_t)c->ovl, (uintptr_t)c->ovl_key, (uintptr_t)c->pkey, (uintptr_t)c->slot_keys,
                           c->ovl_cap};
@@ -881,7 +882,7 @@ int32_t gr_context_destroy(gr_context* c) {
   dev_free(c->d_texs); dev_free(c->d_tables);
   if (c->h_tables) cudaFreeHost(c->h_tables);
   dev_free(c->rast); dev_free(c->shade); dev_free(c->suv); dev_free(c->wide); dev_free(c->tcol);
-  dev_free(c->rec_of_key); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->tile_info);
+  dev_free(c->rec_of_face); dev_free(c->bins); dev_free(c->bin_count); dev_free(c->tile_cost); dev_free(c->tile_info);
   dev_free(c->big);
   dev_free(c->gkey); dev_free(c->tile_done); dev_free(c->clip); dev_free(c->kept); dev_free(c->vlight);
   dev_free(c->vclip); dev_free(c->vscr);

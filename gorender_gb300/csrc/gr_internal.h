@@ -14,6 +14,7 @@ constexpr int kMaxDim = 16384;                // narrow edge-function bound
 constexpr int kNarrowLimit = 16384;           // |screen coordinate| < 2^14 => int32 edge math
 constexpr int kMaxFan = 7;                    // a triangle clipped by 6 planes fans into <= 7
 constexpr int kKeysPerFace = 8;               // order key = face * 8 + fan + 1
+constexpr uint32_t kClipFace = 0x80000000u;   // rec_of_face: a clipped face, the low bits its first fan record
 constexpr int kProjectThreads = 256;
 // k_cull (and k_vertex / k_light): faces (vertices, normals) a thread, 1, 2
 // or 4 by the frame's face count
@@ -37,7 +38,6 @@ __host__ __device__ constexpr int setup_ctas_per_sm(int project_g) { return proj
 __host__ __device__ constexpr int setup_blocks_max(int project_g) { return setup_ctas_per_sm(project_g) * 152; }
 constexpr int kClipBlocks = 2 * 152;          // k_clip grid (grid-stride over the queue)
 constexpr int kBigBlocks = 3 * 152;           // k_bin_big / k_overlay grid (grid-stride over the queue)
-constexpr int kClearBlocks = 8 * 152;         // k_clear grid (grid-stride over the empty tiles)
 
 // Texture table entry (texture.go:19-26).
 struct DevTex {
@@ -209,7 +209,7 @@ struct DevWork {
   unsigned int plan_front, plan_back;  // raster work items: split tiles, whole tiles
   unsigned int raster_next, raster_exit;  // persistent raster: next item, finished CTAs
   unsigned int novl, ovl_need;      // overlay records written / needed
-  unsigned int nempty, clear_exit;  // empty tiles for k_clear; its finished CTAs (it resets both)
+  unsigned int nempty, clear_next;  // tiles without bin entries (k_plan); the next one k_raster clears
   unsigned int nkept;               // faces k_cull kept whole, for k_setup
 };
 
@@ -234,7 +234,6 @@ struct FrameArgs {
   uint32_t bin_cap;
   uint32_t rec_cap;
   uint32_t big_cap;
-  uint32_t key_cap;
   const DevItem* items;
   const DevTex* texs;
   int num_tex;
@@ -243,7 +242,9 @@ struct FrameArgs {
   TriUV* suv;                       // read only for textured triangles (TriShade::tex >= 0)
   TriWide* wide;
   TriColor* tcol;
-  uint32_t* rec_of_key;             // order key -> record index
+  uint32_t* rec_of_face;            // per global face: its record (a face kept whole) or kClipFace |
+                                    // the first record of its fans (a clipped face: fan k at first + k)
+  uint32_t face_cap;
   uint32_t* bins;                   // tiles x bin_cap record indices
   uint32_t* bin_count;              // per tile: entries
   uint32_t* tile_cost;              // per tile: tile-clipped box pixels of entries larger than kSmallBox
@@ -269,9 +270,9 @@ struct FrameArgs {
   unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)
   unsigned long long* view_tpf_out; // per view: published by k_plan
   uint2* plan;                      // raster work items (tile, slice | view << 5), plan_cap entries
-  uint2* empty_tiles;               // (tile, view) of tiles without bin entries, shaded by k_clear
+  uint2* empty_tiles;               // (tile, view) of tiles without bin entries, cleared by k_raster
   uint32_t empty_cap;
-  int clear_empty;                  // nonzero: tiles without bin entries go to k_clear (batches
+  int clear_empty;                  // nonzero: tiles without bin entries go to that list (batches
                                     // shaded in place), not to the raster queue
   uint32_t plan_cap;
   int raster_ctas;                  // persistent raster grid

@@ -501,6 +501,7 @@ __device__ __forceinline__ void face_attributes(const FrameArgs& a, const DevIte
 }
 
 // Writes record r of a set-up triangle (raster part, int64 edges, shading).
+// The caller records where the resolve finds it (rec_of_face).
 __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Setup& s, const SV& q0, const SV& q1,
                                              const SV& q2, int tex, uint32_t okey, bool from_kept = false) {
   s.r.key = okey | (s.wide ? 0x80000000u : 0u);
@@ -531,7 +532,14 @@ __device__ __forceinline__ void write_record(const FrameArgs& a, uint32_t r, Set
     c->c[3] = q1.r; c->c[4] = q1.g; c->c[5] = q1.b;
     c->c[6] = q2.r; c->c[7] = q2.g; c->c[8] = q2.b;
   }
-  if (okey < a.key_cap) a.rec_of_key[okey] = r;
+}
+
+// Record index of the triangle with order key okey (face * 8 + fan + 1): a
+// face kept whole maps to its record, a clipped face to the first record of
+// its fans, which lie side by side in fan order.
+__device__ __forceinline__ uint32_t record_of_key(const FrameArgs& a, uint32_t okey) {
+  const uint32_t e = a.rec_of_face[okey / (uint32_t)kKeysPerFace];
+  return (e & kClipFace) ? (e & ~kClipFace) + (okey % (uint32_t)kKeysPerFace - 1u) : e;
 }
 
 // Binning without warp aggregation (the rare clipped path): up to
@@ -753,9 +761,11 @@ __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
 // warp's faces may belong to different items and views.
 // ---------------------------------------------------------------------------
 // CTAS resident CTAs an SM (setup_ctas_per_sm): 2 measured 3 us less than 4
-// CTAs with spills on a 200k-face frame.
+// CTAs with spills on a 200k-face frame.  Registers are capped at 104 with 2
+// CTAs (2 x 256 x 104 = 53,248: a 96-register k_clip CTA still fits beside
+// them, as k_clip runs beside k_setup) and at 80 with 3 (3 x 256 x 80).
 template <int CTAS>
-__global__ void __launch_bounds__(kProjectThreads, CTAS) k_setup(const FrameArgs a) {
+__global__ void __maxnreg__(CTAS == 3 ? 80 : 104) k_setup(const FrameArgs a) {
   griddep_wait();
   const uint32_t nkept = min(*(volatile uint32_t*)&a.work->nkept, a.kept_cap);
   const unsigned lane = lane_id();
@@ -814,6 +824,7 @@ __global__ void __launch_bounds__(kProjectThreads, CTAS) k_setup(const FrameArgs
     int pbx0 = 0, pbx1 = -1, pby0 = 0, pby1 = -1;  // the record's pixel box
     if (ok) {
       write_record(a, r, s, s0, s1, s2, tex, okey, true);
+      if (okey / (uint32_t)kKeysPerFace < a.face_cap) a.rec_of_face[okey / (uint32_t)kKeysPerFace] = r;
       pbx0 = s.r.bx0; pbx1 = s.r.bx1; pby0 = s.r.by0; pby1 = s.r.by1;
       tx0 = (uint32_t)s.r.bx0 >> a.tile_shift;
       tx1 = (uint32_t)s.r.bx1 >> a.tile_shift;
@@ -910,7 +921,11 @@ __device__ __forceinline__ SV shfl_sv(const SV& v, int src) {
   return o;
 }
 
-__global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
+// Capped at 96 registers (128 threads a CTA): k_clip runs beside k_setup,
+// and one of its CTAs (12,288 registers) then fits beside two k_setup<2> CTAs
+// (2 x 26,624) on an SM; at 104+ registers it waited for k_setup's CTAs to
+// leave, and k_plan waited for it (same-box A/B: heightfield +5 us).
+__global__ void __maxnreg__(96) k_clip(const FrameArgs a) {
   griddep_wait();
   const uint32_t nclip = min(*(volatile uint32_t*)&a.work->nclip, a.clip_cap);
   const uint32_t nkept = *(volatile uint32_t*)&a.work->nkept;
@@ -999,18 +1014,30 @@ __global__ void __launch_bounds__(128) k_clip(const FrameArgs a) {
     int ntpf = 0;
     bool many = false;  // spans more than kBinDirectMax tiles: binned by the warp below
     uint32_t rr = 0;
+    Setup s;
+    bool emit = false;
     if (fan && bin_test(s0, s1, s2, (float)vw.W, (float)vw.H)) {
       ntpf = 1;
-      Setup s;
-      if ((vw.flags & 0x02u) && setup_tri(s0, s1, s2, vw.W, vw.H, s)) {
-        const uint32_t r = nkept + atomicAdd(&a.work->nrec, 1u);  // after the kept faces' records
-        if (r < a.rec_cap) {
-          write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
-          many = bin_record_direct(a, r, s.r, it.view);
-          rr = r;
-        } else {
-          atomicMax(&a.work->rec_need, r + 1);
-        }
+      emit = (vw.flags & 0x02u) && setup_tri(s0, s1, s2, vw.W, vw.H, s);
+    }
+    // The face's fan records are consecutive, after the kept faces' records:
+    // one slot a fan (a fan that yields no record leaves its slot unused), so
+    // the resolve finds fan k at the first record + k.
+    const unsigned em = __ballot_sync(FULL_MASK, emit);
+    if (em) {
+      uint32_t first = 0;
+      if (lane == 0) {
+        first = nkept + atomicAdd(&a.work->nrec, (uint32_t)(count - 2));
+        if (it.face_base + (uint32_t)f < a.face_cap) a.rec_of_face[it.face_base + (uint32_t)f] = kClipFace | first;
+      }
+      first = __shfl_sync(FULL_MASK, first, 0);
+      const uint32_t r = first + (uint32_t)lane;
+      if (emit && r < a.rec_cap) {
+        write_record(a, r, s, s0, s1, s2, tex, (it.face_base + (uint32_t)f) * (uint32_t)kKeysPerFace + (uint32_t)lane + 1u);
+        many = bin_record_direct(a, r, s.r, it.view);
+        rr = r;
+      } else if (emit) {
+        atomicMax(&a.work->rec_need, r + 1);
       }
     }
     // Fan triangles over many tiles, one at a time by the whole warp, so that
@@ -1388,7 +1415,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
       out_z = 0.0f;
       return;
     }
-    const uint32_t r = a.rec_of_key[okey];
+    const uint32_t r = record_of_key(a, okey);
     const TriRaster t = unpack_tri(a, r, vw.W, vw.H);
     bool inside;
     float e12f, e20f, al, be, ga;
@@ -1825,8 +1852,8 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   // heavy items (split tiles, or whole tiles worth half a slice) go to the
   // front of the queue so that they start first; the rest to the back
   const bool heavy = ns > 1 || cost >= a.slice_cost / 2u;
-  // A tile without bin entries of a batch shaded in place goes to k_clear's
-  // list instead of the raster queue: all background, no keys.
+  // A tile without bin entries of a batch shaded in place goes to the list
+  // of tiles to clear instead of the raster queue: all background, no keys.
   const bool clear = count == 0 && a.clear_empty;
   uint32_t mf = 0, mb = 0, me = 0;
   if (valid) {
@@ -1862,13 +1889,19 @@ __global__ void __launch_bounds__(256) k_plan(const FrameArgs a) {
   }
 }
 
-// Persistent raster: CTAs take work items from the queue until it is empty;
-// the last CTA to finish publishes and resets the frame's counters.
 template <int TS>
+__device__ __forceinline__ void clear_quad(const FrameArgs& a, uint2 e, uint32_t qq);
+
+// Persistent raster: CTAs take work items from the queue until it is empty;
+// the last CTA to finish publishes and resets the frame's counters.  CLEAR:
+// the frame's tiles without bin entries are cleared here too (batches shaded
+// in place; a separate instantiation, so the other frames' raster keeps its
+// registers free of the clear loop).
+template <int TS, bool CLEAR>
 __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kMinBlocks) k_raster(const FrameArgs a) {
   griddep_wait();
   __shared__ RasterSmem<TS> sm;
-  __shared__ uint32_t s_item, s_tile, s_slice, s_lastcta;
+  __shared__ uint32_t s_item, s_tile, s_slice, s_lastcta, s_clear;
   __shared__ int s_view;
   const uint32_t front = *(volatile uint32_t*)&a.work->plan_front;
   const uint32_t total = front + *(volatile uint32_t*)&a.work->plan_back;
@@ -1889,6 +1922,24 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     if (s_item >= total) break;
     raster_item<TS>(a, s_tile, s_slice, s_view, sm);
     __syncthreads();  // shared memory is reused by the next item
+  }
+  // Tiles without bin entries (batches shaded in place, k_plan's list): once
+  // the raster queue is empty, the CTAs clear them, kClearGrab tiles a grab,
+  // one four-pixel group a thread a tile (TS x TS / 4 = the CTA's threads).
+  // Their stores fill the raster's tail instead of a kernel of their own,
+  // which could not share an SM with this one (its registers fill the SM).
+  if constexpr (CLEAR) {
+    constexpr uint32_t kClearGrab = 4;
+    const uint32_t ne = min(*(volatile uint32_t*)&a.work->nempty, a.empty_cap);
+    for (;;) {
+      // s_clear, not s_item: a warp may still be reading s_item for the loop above
+      if (threadIdx.x == 0) s_clear = atomicAdd(&a.work->clear_next, kClearGrab);
+      __syncthreads();
+      const uint32_t e0 = s_clear;
+      __syncthreads();  // s_clear is written again by the next grab
+      if (e0 >= ne) break;
+      for (uint32_t e = e0; e < min(ne, e0 + kClearGrab); ++e) clear_quad<TS>(a, a.empty_tiles[e], threadIdx.x);
+    }
   }
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1917,6 +1968,7 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     w->tpf = 0; w->nrec = 0; w->nbig = 0; w->bin_need = 0; w->rec_need = 0; w->big_need = 0; w->error = 0;
     w->nclip = 0; w->clip_need = 0; w->max_bin = 0; w->nkept = 0;
     w->plan_front = 0; w->plan_back = 0; w->raster_next = 0; w->raster_exit = 0;
+    w->nempty = 0; w->clear_next = 0;
   }
   __syncthreads();
   for (int v = threadIdx.x; v < a.num_views; v += blockDim.x) {
@@ -1972,27 +2024,20 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_clear: the tiles without bin entries of frames shaded in place (k_plan's
-// list), four pixels a thread over all of them, beside k_raster: Clear and
-// DotGrid (rasterizer.go:36-52), overlay marks, crosshair and fog through
-// resolve_pixel with the background key.  The last CTA to finish returns the
-// list's counter to zero for the next frame.
+// Tiles without bin entries of frames shaded in place (k_plan's list), which
+// k_raster<TS, true> clears once its queue is empty.
 // ---------------------------------------------------------------------------
+// Four-pixel group qq of tile e (tile, view) without bin entries: Clear and
+// DotGrid (rasterizer.go:36-52), overlay marks, crosshair and fog through
+// resolve_pixel with the background key.
 template <int TS>
-__global__ void __launch_bounds__(256) k_clear(const FrameArgs a) {
-  __shared__ uint32_t s_last;
-  constexpr uint32_t kQuads = TS * TS / 4;  // four-pixel groups a tile
-  const uint32_t ne = min(*(volatile uint32_t*)&a.work->nempty, a.empty_cap);
-  const unsigned long long total = (unsigned long long)ne * kQuads;
-  for (unsigned long long q = (unsigned long long)blockIdx.x * 256u + threadIdx.x; q < total;
-       q += (unsigned long long)gridDim.x * 256u) {
-    const uint2 e = a.empty_tiles[q / kQuads];
-    const uint32_t qq = (uint32_t)(q % kQuads);
+__device__ __forceinline__ void clear_quad(const FrameArgs& a, uint2 e, uint32_t qq) {
+  {
     const DevView& vw = a.views[e.y];
     const uint32_t lt = e.x - vw.tile_base;
     const int x = (int)(lt % (uint32_t)vw.tiles_x) * TS + (int)(qq % (TS / 4)) * 4;
     const int y = (int)(lt / (uint32_t)vw.tiles_x) * TS + (int)(qq / (TS / 4));
-    if (y >= vw.H) continue;
+    if (y >= vw.H) return;
     uint32_t c[4];
     float z[4];
     if (!(vw.flags & (0xC0u | 0x100u | kViewFaceIds)) && !vw.fog_on) {
@@ -2026,16 +2071,6 @@ __global__ void __launch_bounds__(256) k_clear(const FrameArgs a) {
       }
     }
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(&a.work->clear_exit, 1u) == gridDim.x - 1 ? 1u : 0u;
-  }
-  __syncthreads();
-  if (s_last && threadIdx.x == 0) {
-    a.work->nempty = 0u;
-    a.work->clear_exit = 0u;
-  }
 }
 
 int raster_grid(int tile_shift, int waves) {
@@ -2043,9 +2078,9 @@ int raster_grid(int tile_shift, int waves) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (tile_shift == 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<16>, RasterShape<16>::kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<16, false>, RasterShape<16>::kThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<32>, RasterShape<32>::kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<32, false>, RasterShape<32>::kThreads, 0);
   return max(1, sms) * max(1, per) * max(1, waves);
 }
 
@@ -2129,21 +2164,15 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
   if (events) k_plan<<<(a.total_tiles + 255) / 256, 256, 0, s>>>(a);
   else launch_after(k_plan, (a.total_tiles + 255) / 256, 256, s, a);
   ++n;
-  const bool clear = a.clear_empty;  // tiles without bin entries, shaded in place by k_clear
-  if (clear) {
-    fork(2);
-    if (a.tile_shift == 4) k_clear<16><<<kClearBlocks, 256, 0, s2>>>(a);
-    else k_clear<32><<<kClearBlocks, 256, 0, s2>>>(a);
-    ++n;
-  }
-  if (a.tile_shift == 4) launch_after(k_raster<16>, a.raster_ctas, RasterShape<16>::kThreads, s, a);
-  else launch_after(k_raster<32>, a.raster_ctas, RasterShape<32>::kThreads, s, a);
+  if (a.tile_shift == 4)
+    launch_after(a.clear_empty ? k_raster<16, true> : k_raster<16, false>, a.raster_ctas, RasterShape<16>::kThreads, s, a);
+  else
+    launch_after(a.clear_empty ? k_raster<32, true> : k_raster<32, false>, a.raster_ctas, RasterShape<32>::kThreads, s, a);
   ++n;
   if (a.pkey && a.total_pixels) {
     launch_after(k_resolve, (unsigned)((a.total_pixels + 255) / 256), 256, s, a);
     ++n;
   }
-  if (clear) join(2);
   if (events) cudaEventRecord((cudaEvent_t)events[3], s);
   if (launches) *launches = n;
   return (int)cudaGetLastError();

@@ -52,7 +52,6 @@ constexpr int kMaxVertices = 32768;
 constexpr int kMaxSide = 512;
 constexpr int kTiles = (kMaxSide / 32) * (kMaxSide / 32);
 constexpr uint32_t kRecCap = 3u * kMaxFaces;
-constexpr uint32_t kKeyCap = (uint32_t)kKeysPerFace * kMaxFaces + kKeysPerFace;
 constexpr uint32_t kBinCap = 1024;
 constexpr uint32_t kQueueCap = kMaxFaces + 1024;
 constexpr size_t kScratchBytes = 8u << 20;
@@ -83,7 +82,7 @@ constexpr Layout make_layout() {
   l.suv = o; o += up256(sizeof(TriUV) * kRecCap);
   l.wide = o; o += up256(sizeof(TriWide) * kRecCap);
   l.tcol = o; o += up256(sizeof(TriColor) * kRecCap);
-  l.keys = o; o += up256(sizeof(uint32_t) * kKeyCap);
+  l.keys = o; o += up256(sizeof(uint32_t) * kMaxFaces);
   l.bins = o; o += up256(sizeof(uint32_t) * kTiles * kBinCap);
   l.bin_count = o; o += up256(sizeof(uint32_t) * kTiles);
   l.tile_cost = o; o += up256(sizeof(uint32_t) * kTiles);
@@ -289,7 +288,6 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.bin_cap = kBinCap;
   a.rec_cap = kRecCap;
   a.big_cap = kQueueCap;
-  a.key_cap = kKeyCap;
   a.clip_cap = kQueueCap;
   a.slice_cost = kDefaultSliceCost;
   a.light_blocks = light_blocks;
@@ -301,7 +299,8 @@ extern "C" int32_t gr_draw_noalloc(int32_t device, const gr_noalloc_object* obje
   a.suv = (TriUV*)(base + kLayout.suv);
   a.wide = (TriWide*)(base + kLayout.wide);
   a.tcol = (TriColor*)(base + kLayout.tcol);
-  a.rec_of_key = (uint32_t*)(base + kLayout.keys);
+  a.rec_of_face = (uint32_t*)(base + kLayout.keys);
+  a.face_cap = kMaxFaces;
   a.bins = (uint32_t*)(base + kLayout.bins);
   a.bin_count = (uint32_t*)(base + kLayout.bin_count);
   a.tile_cost = (uint32_t*)(base + kLayout.tile_cost);
