@@ -367,6 +367,13 @@ __device__ __forceinline__ unsigned long long depth_key(float z, uint32_t okey) 
 }
 #define BG_KEY 0x407fffff00000000ULL  // depth_key(-1.0f, 0): ~0xbf800000 = 0x407fffff
 
+// The zRec bits of visibility key k (the inverse of depth_key's order map);
+// +0 also stands for a zRec of -0, which depth_key folds onto it.
+__device__ __forceinline__ float key_depth(unsigned long long k) {
+  const uint32_t o = (uint32_t)(k >> 32);
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
 // Barycentrics and zRec at a covered pixel (rasterizer.go:149-153).
 __device__ __forceinline__ float zrec_of(float e12f, float e20f, float sumf, float w0, float w1, float w2,
                                          float& al, float& be, float& ga) {
@@ -1420,7 +1427,19 @@ __device__ __forceinline__ void resolve_pixel(const FrameArgs& a, const DevView&
     bool inside;
     float e12f, e20f, al, be, ga;
     edges_at(t, a.wide, r, x, y, inside, e12f, e20f);
-    const float z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
+    // The winner's zRec is the depth its key holds (the raster computed it
+    // from the same record at this pixel): only the barycentrics are divided
+    // out again.  A key depth of +0 may stand for -0, so that case takes the
+    // full zRec.
+    float z;
+    if ((uint32_t)(k >> 32) != 0x80000000u) {
+      al = fd(e12f, t.sumf);
+      be = fd(e20f, t.sumf);
+      ga = fs(fs(1.0f, al), be);
+      z = key_depth(k);
+    } else {
+      z = zrec_of(e12f, e20f, t.sumf, t.w0, t.w1, t.w2, al, be, ga);
+    }
     out_z = z;
     const TriShade s = a.shade[r];
     const float I = fa(fa(fm(al, s.i0), fm(be, s.i1)), fm(ga, s.i2));
@@ -1929,16 +1948,19 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
   // Their stores fill the raster's tail instead of a kernel of their own,
   // which could not share an SM with this one (its registers fill the SM).
   if constexpr (CLEAR) {
-    constexpr uint32_t kClearGrab = 4;
+    constexpr uint32_t kClearGrab = 8;
     const uint32_t ne = min(*(volatile uint32_t*)&a.work->nempty, a.empty_cap);
+    // s_clear, not s_item: a warp may still be reading s_item for the loop above
+    if (threadIdx.x == 0) s_clear = atomicAdd(&a.work->clear_next, kClearGrab);
+    __syncthreads();
     for (;;) {
-      // s_clear, not s_item: a warp may still be reading s_item for the loop above
-      if (threadIdx.x == 0) s_clear = atomicAdd(&a.work->clear_next, kClearGrab);
-      __syncthreads();
       const uint32_t e0 = s_clear;
-      __syncthreads();  // s_clear is written again by the next grab
+      __syncthreads();  // every thread has read this grab
       if (e0 >= ne) break;
+      // the next grab's atomic is in flight while these tiles are cleared
+      if (threadIdx.x == 0) s_clear = atomicAdd(&a.work->clear_next, kClearGrab);
       for (uint32_t e = e0; e < min(ne, e0 + kClearGrab); ++e) clear_quad<TS>(a, a.empty_tiles[e], threadIdx.x);
+      __syncthreads();  // the next grab is in s_clear
     }
   }
   if (threadIdx.x == 0) {
