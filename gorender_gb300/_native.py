@@ -29,7 +29,8 @@ STATUS_NAMES = {0: "GR_OK", 1: "GR_ERR_INVALID_ARGUMENT", 2: "GR_ERR_CUDA", 3: "
 EXPORTS = [
     "gr_last_error", "gr_version", "gr_context_create", "gr_context_destroy", "gr_context_sync",
     "gr_mesh_create", "gr_mesh_destroy", "gr_mesh_bounding_box", "gr_texture_create", "gr_draw",
-    "gr_draw_async", "gr_object_matrices", "gr_screen_matrix", "gr_normalize3", "gr_mesh_face_normals",
+    "gr_draw_async", "gr_object_matrices", "gr_screen_matrix", "gr_normalize3", "gr_box_visibility",
+    "gr_mesh_face_normals",
     "gr_renderer_create", "gr_renderer_destroy", "gr_renderer_set_flags", "gr_renderer_get_flags",
     "gr_renderer_set_fov", "gr_renderer_set_light", "gr_renderer_draw", "gr_renderer_read",
     "gr_renderer_tpf", "gr_context_event_record", "gr_context_event_elapsed", "gr_context_flush_l2",
@@ -136,6 +137,7 @@ def lib() -> C.CDLL:
             "gr_object_matrices": [C.POINTER(Object), C.POINTER(Camera), i32, i32, C.c_float, fp, fp],
             "gr_screen_matrix": [i32, i32, fp],
             "gr_normalize3": [fp, fp],
+            "gr_box_visibility": [fp, fp, vp],
             "gr_mesh_face_normals": [vp, i32, vp, i32, vp],
             "gr_renderer_create": [vp, i32, i32, C.POINTER(vp)],
             "gr_renderer_destroy": [vp],

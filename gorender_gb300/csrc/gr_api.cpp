@@ -1455,6 +1455,12 @@ int32_t gr_normalize3(const float* v, float* out) {
   return GR_OK;
 }
 
+int32_t gr_box_visibility(const float* mvp, const float* bbox, int32_t* out) {
+  if (!mvp || !bbox || !out) return fail(GR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = box_visibility(mvp, bbox);
+  return GR_OK;
+}
+
 int32_t gr_mesh_face_normals(const float* pos, int32_t nv, const int32_t* vidx, int32_t nf, float* out) {
   if (!pos || !vidx || !out || nv <= 0 || nf < 0) return fail(GR_ERR_INVALID_ARGUMENT, "bad argument");
   for (long i = 0; i < 3L * nf; ++i)

@@ -200,6 +200,12 @@ int32_t gr_object_matrices(const gr_object* obj, const gr_camera* cam, int32_t w
 int32_t gr_screen_matrix(int32_t width, int32_t height, float* out16);
 /* Vec3.Normalize (vector.go:78-80). */
 int32_t gr_normalize3(const float* v3, float* out3);
+/* Frustum.BoxVisibility (clipping.go:131-154) of a mesh's bounding box
+ * (Mesh.BoundingBox: 8 corners x 4 floats, mesh.go:28-51) transformed by mvp
+ * as projectObject does (renderer.go:268-275), zNear 0 and zFar 50: *out =
+ * 0 outside, 1 intersecting, 2 inside.  gr_draw computes it once per draw
+ * item with this same function; k_cull skips the faces of an object outside. */
+int32_t gr_box_visibility(const float* mvp16, const float* bbox32, int32_t* out);
 /* NewMesh face normals (mesh.go:55-60): num_faces x 4 floats. */
 int32_t gr_mesh_face_normals(const float* positions, int32_t num_vertices,
                              const int32_t* vertex_indices, int32_t num_faces, float* out);

@@ -98,6 +98,58 @@ def test_object_matrices_match_oracle_large_and_demo_angles():
         assert np.array_equal(world.view(np.uint32), world2.view(np.uint32)), a
 
 
+def _box_corners(lo, hi):
+    """Mesh.BoundingBox's 8 corners (x outermost, then y, then z; w = 1)."""
+    c = np.zeros((8, 4), np.float32)
+    for k in range(8):
+        c[k] = [hi[0] if k & 4 else lo[0], hi[1] if k & 2 else lo[1], hi[2] if k & 1 else lo[2], 1.0]
+    return c
+
+
+def test_box_visibility_matches_oracle():
+    """Frustum.BoxVisibility of a transformed bounding box (clipping.go:131-154,
+    renderer.go:268-275), which gr_draw now decides on the host for each draw
+    item: the library's function against the oracle's transform + classify,
+    on object matrices around a camera (boxes inside, straddling each plane,
+    behind the camera, beyond zFar) and on raw matrices with extreme and
+    non-finite entries."""
+    L = N.lib()
+    O = oracle.lib()
+    rng = np.random.default_rng(23)
+    seen = set()
+
+    def fptr(a):
+        return a.ctypes.data_as(C.POINTER(C.c_float))
+
+    def check(mvp, box):
+        mvp = np.ascontiguousarray(mvp, np.float32)
+        box = np.ascontiguousarray(box, np.float32)
+        out = C.c_int32()
+        assert L.gr_box_visibility(fptr(mvp), fptr(box), C.byref(out)) == N.GR_OK
+        corners = box.copy()  # the oracle transforms the corners in place, then classifies them
+        O.orc_transform_batch(fptr(mvp), fptr(corners), 8)
+        ref = O.orc_box_visibility(fptr(corners), C.c_float(0.0), C.c_float(50.0))
+        assert out.value == ref, (mvp, box, out.value, ref)
+        seen.add(ref)
+
+    for _ in range(3000):
+        s = rng.uniform(0.05, 4.0, 3).astype(np.float32)
+        r = rng.uniform(-3, 3, 3).astype(np.float32)
+        t = rng.uniform(-30, 30, 3).astype(np.float32)
+        eye = rng.uniform(-10, 10, 3).astype(np.float32)
+        d = rng.normal(size=3).astype(np.float32)
+        fov = oracle.fov_radians(float(rng.uniform(30, 90)))
+        mvp, _ = gr.object_matrices(s, r, t, eye, d, (0, 1, 0), 1280, 720, fov)
+        lo = rng.uniform(-2, 0, 3).astype(np.float32)
+        check(mvp, _box_corners(lo, lo + rng.uniform(0, 3, 3).astype(np.float32)))
+    assert seen == {0, 1, 2}
+    for _ in range(500):
+        mvp = rng.normal(size=16).astype(np.float32) * np.float32(10.0) ** rng.integers(-6, 7, 16)
+        mvp[rng.integers(0, 16)] = rng.choice([np.inf, -np.inf, np.nan, 0.0, 1e38])
+        lo = rng.uniform(-1e3, 1e3, 3).astype(np.float32)
+        check(mvp, _box_corners(lo, lo + np.float32(rng.uniform(0, 1e3))))
+
+
 def test_screen_matrix_light_fov_match_oracle():
     for w, h in [(640, 360), (1280, 720), (1920, 1080), (643, 357)]:
         assert np.array_equal(gr.screen_matrix(w, h), oracle.screen_matrix(w, h))
