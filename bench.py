@@ -150,7 +150,7 @@ STAGES = {"project_stage": "k_light + k_vertex + k_cull + k_clip + k_setup",
           "raster_stage": "k_plan + k_raster + k_resolve (one view) or k_plan + k_raster, which also clears the empty tiles (a batch)"}
 STAGE_KERNELS = {"project_stage": ["k_light", "k_vertex", "k_cull", "k_clip", "k_setup"],
                  "bin_stage": ["k_bin_big", "k_overlay"],
-                 "raster_stage": ["k_plan", "k_raster", "k_resolve", "k_clear"],
+                 "raster_stage": ["k_plan", "k_raster", "k_resolve"],
                  "forward": ["k_diff_vertices", "k_diff_tables", "k_diff_shade"],
                  "backward": ["k_diff_grad", "k_diff_scatter"]}
 
