@@ -1203,7 +1203,7 @@ int32_t cold_l2(gr_context* c, int seed) {
 struct TuneCfg {
   int shift, slice, waves;
 };
-constexpr TuneCfg kTuneCands[] = {{5, 8192, 1}, {5, 16384, 1}, {5, 32768, 1}, {5, 65536, 1},
+constexpr TuneCfg kTuneCands[] = {{5, 8192, 1}, {5, 16384, 1}, {5, 32768, 1}, {5, 65536, 1}, {5, 131072, 1},
                                   {4, 2048, 1}, {4, 4096, 1}, {4, 8192, 1}, {4, 16384, 1}};
 
 // Runs `run(ms)` (one timed draw that also sizes the buffers) for every
