@@ -2028,15 +2028,15 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameArgs a) {
   const DevView& vw = a.views[v];
   const uint32_t o = (uint32_t)(p - vw.pix_base);
   const int y = (int)(o / (uint32_t)vw.W), x = (int)(o - (uint32_t)y * (uint32_t)vw.W);
-  unsigned long long k;
+  // The pixel's key is loaded beside its tile's info rather than after it (a
+  // split tile, keyed in slots, ignores it): one dependent load less a pixel.
+  unsigned long long k = a.pkey[p];
   const int sh = a.tile_shift, ts = 1 << sh;
   const uint4 ti = a.tile_info[vw.tile_base + (uint32_t)(y >> sh) * (uint32_t)vw.tiles_x + (uint32_t)(x >> sh)];
   if (ti.y > 1 && ti.z != kNoSlot) {  // a split tile: the max over its slices' slots
     const unsigned long long* sk = a.slot_keys + (size_t)ti.z * (size_t)(ts * ts) + (size_t)((y & (ts - 1)) * ts + (x & (ts - 1)));
     k = sk[0];
     for (uint32_t s = 1; s < ti.y; ++s) k = max(k, sk[(size_t)s * (size_t)(ts * ts)]);
-  } else {
-    k = a.pkey[p];
   }
   uint32_t c;
   float z;
