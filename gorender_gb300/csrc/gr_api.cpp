@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -67,6 +68,8 @@ constexpr int kFrameGraphs = 4;
 struct FrameGraph {
   cudaGraphExec_t exec = nullptr;
   FrameArgs args{};
+  const void* copy_src = nullptr;   // the table upload captured as the graph's first node (or none)
+  size_t copy_bytes = 0;
   int launches = 0;
   uint64_t used = 0;
 };
@@ -251,7 +254,7 @@ int32_t ensure_tables(gr_context* c, int nviews, int nitems) {
   const size_t stride = (off + sizeof(DevItem) * (size_t)icap + 255) & ~(size_t)255;
   int32_t st = dev_alloc(&c->d_tables, stride);
   if (st) return st;
-  CK(cudaMallocHost((void**)&c->h_tables, stride * kStageSlots));
+  CK(cudaMallocHost((void**)&c->h_tables, stride * (kStageSlots + 1)));  // + the synchronous draws' slot
   c->tables_off = off;
   c->tables_stride = stride;
   c->d_views = reinterpret_cast<DevView*>(c->d_tables);
@@ -377,6 +380,8 @@ int32_t upload_textures(gr_context* c) {
 
 struct Prepared {
   FrameArgs a;
+  const void* copy_src = nullptr;   // synchronous draws: the tables' page-locked source, uploaded by the
+  size_t copy_bytes = 0;            // frame's graph (no separate copy)
   uint64_t faces;
   int nitems;
 };
@@ -419,7 +424,7 @@ int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
 // Validates views and items, stages the view and item tables and fills the
 // kernel arguments.  items[i].reserved is the item's view when batched.
 int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_item* items, int32_t n, bool batched,
-                Prepared& out, DevView* own_views = nullptr, DevItem* own_items = nullptr) {
+                Prepared& out, DevView* own_views = nullptr, DevItem* own_items = nullptr, bool sync_slot = false) {
   if (nviews <= 0 || !views) return fail(GR_ERR_INVALID_ARGUMENT, "no views");
   if (n < 0 || (n > 0 && !items)) return fail(GR_ERR_INVALID_ARGUMENT, "bad item list");
   const int ts = 1 << c->tile_shift;
@@ -469,8 +474,12 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
       return st;
     c->pkey_pixels = total_pixels;
   }
-  const int slot = (c->stage_slot + 1) % kStageSlots;
-  if (c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
+  // Synchronous draws stage in a slot of their own (the previous one has
+  // finished), uploaded by the frame's graph; the others rotate through the
+  // ring, each slot reused once the copy that read it has run.
+  const bool in_graph = sync_slot && !own_views && !own_items;
+  const int slot = in_graph ? kStageSlots : (c->stage_slot + 1) % kStageSlots;
+  if (!in_graph && c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
   unsigned char* hslot = c->h_tables + (size_t)slot * c->tables_stride;
   DevView* hviews = reinterpret_cast<DevView*>(hslot);
   DevItem* hitems = reinterpret_cast<DevItem*>(hslot + c->tables_off);
@@ -584,7 +593,12 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // a graph batch keeps its own tables, so other draws cannot overwrite them
   DevView* dviews = own_views ? own_views : c->d_views;
   DevItem* ditems = own_items ? own_items : c->d_items;
-  if (!own_views && !own_items) {  // both tables with one copy
+  if (in_graph) {  // both tables with one copy, the first node of the frame's graph
+    const size_t bytes = live ? c->tables_off + sizeof(DevItem) * (size_t)live : sizeof(DevView) * (size_t)nviews;
+    out.copy_src = hslot;
+    out.copy_bytes = bytes;
+    c->h2d_bytes = (int64_t)bytes;
+  } else if (!own_views && !own_items) {  // both tables with one copy
     const size_t bytes = live ? c->tables_off + sizeof(DevItem) * (size_t)live : sizeof(DevView) * (size_t)nviews;
     CK(cudaMemcpyAsync(c->d_tables, hslot, bytes, cudaMemcpyHostToDevice, c->stream));
     c->h2d_bytes = (int64_t)bytes;
@@ -593,9 +607,11 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     if (live) CK(cudaMemcpyAsync(ditems, hitems, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
     c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
   }
-  CK(cudaEventRecord(c->stage_ev[slot], c->stream));
-  c->stage_used[slot] = true;
-  c->stage_slot = slot;
+  if (!in_graph) {
+    CK(cudaEventRecord(c->stage_ev[slot], c->stream));
+    c->stage_used[slot] = true;
+    c->stage_slot = slot;
+  }
   c->d2h_bytes = 0;
 
   FrameArgs& a = out.a;
@@ -678,14 +694,16 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
 // device tables), so each launch sequence is captured once into a CUDA graph
 // and replayed; a few are kept (least recently used goes first), so a caller
 // alternating between scenes replays too.
-int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr) {
+int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr, const void* copy_src = nullptr,
+               size_t copy_bytes = 0) {
   int big_blocks = kBigBlocks;
   if (!events) {
     ++c->frame_tick;
     int victim = 0;
     for (int k = 0; k < kFrameGraphs; ++k) {
       FrameGraph& fg = c->frame_graphs[k];
-      if (fg.exec && std::memcmp(&a, &fg.args, sizeof(a)) == 0) {
+      if (fg.exec && fg.copy_src == copy_src && fg.copy_bytes == copy_bytes &&
+          std::memcmp(&a, &fg.args, sizeof(a)) == 0) {
         CK(cudaGraphLaunch(fg.exec, c->stream));
         fg.used = c->frame_tick;
         c->last_launches = fg.launches;
@@ -699,11 +717,15 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
     cudaGraph_t g = nullptr;
     int n = 0;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      const int err = launch_frame(a, big_blocks, c->stream, &n, nullptr, &c->aux);
+      int err = 0;
+      if (copy_bytes) err = (int)cudaMemcpyAsync(c->d_tables, copy_src, copy_bytes, cudaMemcpyHostToDevice, c->stream);
+      if (!err) err = launch_frame(a, big_blocks, c->stream, &n, nullptr, &c->aux);
       const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (!err && e == cudaSuccess && g && cudaGraphInstantiate(&fg.exec, g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
         std::memcpy(&fg.args, &a, sizeof(a));
+        fg.copy_src = copy_src;
+        fg.copy_bytes = copy_bytes;
         fg.launches = n;
         fg.used = c->frame_tick;
         CK(cudaGraphLaunch(fg.exec, c->stream));
@@ -715,6 +737,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr)
       cudaGetLastError();  // capture failed: fall back to plain launches
     }
   }
+  if (copy_bytes) CK(cudaMemcpyAsync(c->d_tables, copy_src, copy_bytes, cudaMemcpyHostToDevice, c->stream));
   int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events, &c->aux);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
   return GR_OK;
@@ -786,12 +809,15 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
     ViewIn v{p, rgba, z};
     v.host_out = rgba_map || z_map;
     Prepared pr;
-    if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
+    if ((st = prepare(c, &v, 1, items, n, false, pr, nullptr, nullptr, true))) return st;
     // the counters and the outputs in one go: one host wait per frame (a frame
     // whose buffers overflowed is drawn again and its outputs copied again);
-    // the last raster CTA writes the counters into page-locked memory itself
+    // the last raster CTA writes the counters into page-locked memory itself,
+    // then sets the done word after them
     pr.a.result_host = c->h_result_dev;
-    if ((st = launch(c, pr.a))) return st;
+    volatile uint32_t* done = reinterpret_cast<volatile uint32_t*>(c->h_result + 1);
+    *done = 0u;
+    if ((st = launch(c, pr.a, nullptr, pr.copy_src, pr.copy_bytes))) return st;
     c->d2h_bytes = (int64_t)sizeof(DevResult);
     if (rgba_out && !rgba_dev) {
       if (!rgba_map) CK(cudaMemcpyAsync(rgba_out, rgba, px * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -801,11 +827,31 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
       if (!z_map) CK(cudaMemcpyAsync(z_out, z, px * 4, cudaMemcpyDeviceToHost, c->stream));
       c->d2h_bytes += (int64_t)px * 4;
     }
-    CK(cudaStreamSynchronize(c->stream));
+    if (!v.host_out || (rgba_out && !rgba_dev && !rgba_map) || (z_out && !z_dev && !z_map)) {
+      // device outputs (k_resolve runs after the raster) or copies after the frame
+      CK(cudaStreamSynchronize(c->stream));
+    } else {
+      // Wait for the done word (counters and outputs are in host memory by
+      // then) rather than for the whole stream; past a second (a fault, or a
+      // device taken by other work) the stream wait decides and reports.
+      bool seen = false;
+      const auto t0 = std::chrono::steady_clock::now();
+      for (uint32_t spins = 0;; ++spins) {
+        if (__atomic_load_n(reinterpret_cast<const uint32_t*>(c->h_result + 1), __ATOMIC_ACQUIRE)) {
+          seen = true;
+          break;
+        }
+        if ((spins & 1023u) == 1023u && std::chrono::steady_clock::now() - t0 > std::chrono::seconds(1)) break;
+      }
+      if (!seen) CK(cudaStreamSynchronize(c->stream));
+    }
     int32_t err;
     const int rerun = check_result(c, *c->h_result, &err);
     if (err) return err;
-    if (rerun) continue;
+    if (rerun) {
+      CK(cudaStreamSynchronize(c->stream));  // before buffers are resized
+      continue;
+    }
     if (tpf_out) *tpf_out = (int64_t)c->h_result->tpf;
     return GR_OK;
   }
@@ -849,7 +895,7 @@ int32_t gr_context_create(int32_t device, gr_context** out) {
   if (e == cudaSuccess) e = cudaMemset(c->work, 0, sizeof(DevWork));
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_result, sizeof(DevResult));
   if (e == cudaSuccess) e = cudaMemset(c->d_result, 0, sizeof(DevResult));
-  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_result, sizeof(DevResult));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_result, 2 * sizeof(DevResult));  // + the done word
   if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c->h_result_dev, c->h_result, 0);
   for (int i = 0; i < 64 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->events[i]);
   for (int i = 0; i < kStageSlots && e == cudaSuccess; ++i)

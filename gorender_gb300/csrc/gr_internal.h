@@ -266,7 +266,9 @@ struct FrameArgs {
   DevWork* work;
   DevResult* result;
   DevResult* result_host;           // device address of page-locked host memory that the last raster
-                                    // CTA copies the result into (null: the host copies it)
+                                    // CTA copies the result into (null: the host copies it), followed
+                                    // by a word it sets to 1 once the frame's writes are visible to the
+                                    // host (every CTA fences at system scope before it retires)
   unsigned long long* view_tpf;     // per view: binned triangles (zeroed by k_plan)
   unsigned long long* view_tpf_out; // per view: published by k_plan
   uint2* plan;                      // raster work items (tile, slice | view << 5), plan_cap entries

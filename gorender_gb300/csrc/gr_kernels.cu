@@ -1964,7 +1964,10 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     }
   }
   if (threadIdx.x == 0) {
-    __threadfence();
+    // outputs in host memory (a synchronous draw): this CTA's writes become
+    // visible to the host before it counts itself done
+    if (a.result_host) __threadfence_system();
+    else __threadfence();
     s_lastcta = atomicAdd(&a.work->raster_exit, 1u) == gridDim.x - 1 ? 1u : 0u;
   }
   __syncthreads();
@@ -2005,6 +2008,11 @@ __global__ void __launch_bounds__(RasterShape<TS>::kThreads, RasterShape<TS>::kM
     if (threadIdx.x < kWords)
       reinterpret_cast<unsigned*>(a.result_host)[threadIdx.x] =
           __ldcg(reinterpret_cast<const unsigned*>(a.result) + threadIdx.x);
+    __syncthreads();
+    if (threadIdx.x == 0) {  // the frame is complete: counters and every output are visible to the host
+      __threadfence_system();
+      reinterpret_cast<volatile unsigned*>(a.result_host)[kWords] = 1u;
+    }
   }
 }
 
