@@ -64,7 +64,10 @@ struct TexRec {
 }  // namespace
 
 namespace {
-constexpr int kFrameGraphs = 4;
+// An asynchronous draw's graph reads the tables from its staging slot, so a
+// scene drawn repeatedly holds one graph per slot: 12 keep four such scenes
+// (or a presenter's two buffers) replaying.
+constexpr int kFrameGraphs = 12;
 struct FrameGraph {
   cudaGraphExec_t exec = nullptr;
   FrameArgs args{};
@@ -380,8 +383,9 @@ int32_t upload_textures(gr_context* c) {
 
 struct Prepared {
   FrameArgs a;
-  const void* copy_src = nullptr;   // synchronous draws: the tables' page-locked source, uploaded by the
-  size_t copy_bytes = 0;            // frame's graph (no separate copy)
+  const void* copy_src = nullptr;   // the tables' page-locked source, uploaded by the frame's graph
+  size_t copy_bytes = 0;            // (Upload::kInGraph, Upload::kRingInGraph; no separate copy)
+  int ring_slot = -1;               // kRingInGraph: the slot whose event the caller records after the launch
   uint64_t faces;
   int nitems;
 };
@@ -421,10 +425,17 @@ int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
   return GR_OK;
 }
 
+// How a draw's tables reach the device: a copy queued by prepare (kCopy),
+// the synchronous draws' own slot read by the frame's graph (kInGraph), or a
+// slot of the ring read by the frame's graph (kRingInGraph: the caller
+// records the slot's event after launching).
+enum class Upload { kCopy, kInGraph, kRingInGraph };
+
 // Validates views and items, stages the view and item tables and fills the
 // kernel arguments.  items[i].reserved is the item's view when batched.
 int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_item* items, int32_t n, bool batched,
-                Prepared& out, DevView* own_views = nullptr, DevItem* own_items = nullptr, bool sync_slot = false) {
+                Prepared& out, DevView* own_views = nullptr, DevItem* own_items = nullptr,
+                Upload upload = Upload::kCopy) {
   if (nviews <= 0 || !views) return fail(GR_ERR_INVALID_ARGUMENT, "no views");
   if (n < 0 || (n > 0 && !items)) return fail(GR_ERR_INVALID_ARGUMENT, "bad item list");
   const int ts = 1 << c->tile_shift;
@@ -477,9 +488,10 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // Synchronous draws stage in a slot of their own (the previous one has
   // finished), uploaded by the frame's graph; the others rotate through the
   // ring, each slot reused once the copy that read it has run.
-  const bool in_graph = sync_slot && !own_views && !own_items;
-  const int slot = in_graph ? kStageSlots : (c->stage_slot + 1) % kStageSlots;
-  if (!in_graph && c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
+  const bool in_graph = upload != Upload::kCopy && !own_views && !own_items;
+  const bool sync_slot = in_graph && upload == Upload::kInGraph;
+  const int slot = sync_slot ? kStageSlots : (c->stage_slot + 1) % kStageSlots;
+  if (!sync_slot && c->stage_used[slot]) CK(cudaEventSynchronize(c->stage_ev[slot]));
   unsigned char* hslot = c->h_tables + (size_t)slot * c->tables_stride;
   DevView* hviews = reinterpret_cast<DevView*>(hslot);
   DevItem* hitems = reinterpret_cast<DevItem*>(hslot + c->tables_off);
@@ -611,6 +623,9 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     CK(cudaEventRecord(c->stage_ev[slot], c->stream));
     c->stage_used[slot] = true;
     c->stage_slot = slot;
+  } else if (!sync_slot) {
+    out.ring_slot = slot;
+    c->stage_slot = slot;
   }
   c->d2h_bytes = 0;
 
@@ -718,7 +733,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr,
     int n = 0;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       int err = 0;
-      if (copy_bytes) err = (int)cudaMemcpyAsync(c->d_tables, copy_src, copy_bytes, cudaMemcpyHostToDevice, c->stream);
+      if (copy_bytes) err = launch_stage(c->d_tables, copy_src, copy_bytes, c->stream);
       if (!err) err = launch_frame(a, big_blocks, c->stream, &n, nullptr, &c->aux);
       const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (!err && e == cudaSuccess && g && cudaGraphInstantiate(&fg.exec, g, 0) == cudaSuccess) {
@@ -737,7 +752,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr,
       cudaGetLastError();  // capture failed: fall back to plain launches
     }
   }
-  if (copy_bytes) CK(cudaMemcpyAsync(c->d_tables, copy_src, copy_bytes, cudaMemcpyHostToDevice, c->stream));
+  if (copy_bytes) CK((cudaError_t)launch_stage(c->d_tables, copy_src, copy_bytes, c->stream));
   int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events, &c->aux);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
   return GR_OK;
@@ -787,6 +802,14 @@ int check_result(gr_context* c, const DevResult& r, int32_t* err) {
   return rerun;
 }
 
+// After a kRingInGraph launch: the slot may be rewritten once this frame has run.
+int32_t record_ring_slot(gr_context* c, const Prepared& pr) {
+  if (pr.ring_slot < 0) return GR_OK;
+  CK(cudaEventRecord(c->stage_ev[pr.ring_slot], c->stream));
+  c->stage_used[pr.ring_slot] = true;
+  return GR_OK;
+}
+
 int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p,
                   uint8_t* rgba_out, float* z_out, int64_t* tpf_out) {
   if (!p) return fail(GR_ERR_INVALID_ARGUMENT, "params is NULL");
@@ -809,7 +832,7 @@ int32_t draw_sync(gr_context* c, const gr_draw_item* items, int32_t n, const gr_
     ViewIn v{p, rgba, z};
     v.host_out = rgba_map || z_map;
     Prepared pr;
-    if ((st = prepare(c, &v, 1, items, n, false, pr, nullptr, nullptr, true))) return st;
+    if ((st = prepare(c, &v, 1, items, n, false, pr, nullptr, nullptr, Upload::kInGraph))) return st;
     // the counters and the outputs in one go: one host wait per frame (a frame
     // whose buffers overflowed is drawn again and its outputs copied again);
     // the last raster CTA writes the counters into page-locked memory itself,
@@ -1092,8 +1115,9 @@ int32_t gr_draw_async(gr_context* c, const gr_draw_item* items, int32_t n, const
   }
   ViewIn v{p, rgba_dev ? (uint32_t*)rgba_dev : c->fb_rgba, z_dev ? z_dev : c->fb_z};
   Prepared pr;
-  if ((st = prepare(c, &v, 1, items, n, false, pr))) return st;
-  return launch(c, pr.a);
+  if ((st = prepare(c, &v, 1, items, n, false, pr, nullptr, nullptr, Upload::kRingInGraph))) return st;
+  if ((st = launch(c, pr.a, nullptr, pr.copy_src, pr.copy_bytes))) return st;
+  return record_ring_slot(c, pr);
 }
 
 int32_t gr_draw_profiled(gr_context* c, const gr_draw_item* items, int32_t n, const gr_frame_params* p,
@@ -2143,9 +2167,10 @@ int32_t presenter_enqueue(gr_presenter* p, int b) {
   CK(cudaStreamWaitEvent(c->stream, p->copied[b], 0));
   ViewIn v{&fp, p->dev[b], r->z};
   Prepared pr;
-  int32_t st = prepare(c, &v, 1, p->items[b].data(), (int32_t)p->items[b].size(), false, pr);
+  int32_t st = prepare(c, &v, 1, p->items[b].data(), (int32_t)p->items[b].size(), false, pr, nullptr, nullptr,
+                       Upload::kRingInGraph);
   if (st) return st;
-  if ((st = launch(c, pr.a))) return st;
+  if ((st = launch(c, pr.a, nullptr, pr.copy_src, pr.copy_bytes)) || (st = record_ring_slot(c, pr))) return st;
   CK(cudaMemcpyAsync(p->res[b], c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaEventRecord(p->rendered[b], c->stream));
   CK(cudaStreamWaitEvent(p->copy, p->rendered[b], 0));

@@ -369,6 +369,10 @@ struct AuxStream {
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
                  const AuxStream* aux = nullptr);
 
+// Copies bytes (rounded up to 16; both buffers are 256-byte strided) from a
+// page-locked staging slot to the device tables with one small kernel.
+int launch_stage(void* dst, const void* src, size_t bytes, void* stream);
+
 // Persistent raster grid: SMs x resident CTAs of k_raster<TS> x waves.
 int raster_grid(int tile_shift, int waves);
 

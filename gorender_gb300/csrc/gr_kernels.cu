@@ -615,6 +615,7 @@ __device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
 // ---------------------------------------------------------------------------
 template <int G>
 __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
+  griddep_wait();  // after k_stage's tables (a no-op without a programmatic launch)
   __shared__ float s_mvp[16];
   __shared__ float s_S[8];
   __shared__ int s_item;
@@ -2103,6 +2104,23 @@ __device__ __forceinline__ void clear_quad(const FrameArgs& a, uint2 e, uint32_t
   }
 }
 
+// k_stage: a draw's tables from their page-locked staging slot (read through
+// its device address, uncached: the host rewrites the slot between frames)
+// into the device tables, as the first kernel of the frame, so the frame's
+// kernels follow a kernel on their stream instead of a copy-engine transfer.
+// One 16-byte word a thread, so the reads that cross to host memory are all
+// in flight at once (a 64-item table is 23.5 KB).
+__global__ void __launch_bounds__(128) k_stage(uint4* __restrict__ dst, const uint4* __restrict__ src, uint32_t n16) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n16) dst[i] = __ldcv(src + i);
+}
+
+int launch_stage(void* dst, const void* src, size_t bytes, void* stream) {
+  const uint32_t n16 = (uint32_t)((bytes + 15) / 16);
+  k_stage<<<(n16 + 127) / 128, 128, 0, (cudaStream_t)stream>>>((uint4*)dst, (const uint4*)src, n16);
+  return (int)cudaGetLastError();
+}
+
 int raster_grid(int tile_shift, int waves) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
@@ -2159,9 +2177,9 @@ int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches
       else k_light<1><<<a.light_blocks, 256, 0, s2>>>(a);
       ++n;
     }
-    if (a.project_g == 4) k_vertex<4><<<a.vert_blocks, 256, 0, s>>>(a);
-    else if (a.project_g == 2) k_vertex<2><<<a.vert_blocks, 256, 0, s>>>(a);
-    else k_vertex<1><<<a.vert_blocks, 256, 0, s>>>(a);
+    if (a.project_g == 4) launch_after(k_vertex<4>, a.vert_blocks, 256, s, a);
+    else if (a.project_g == 2) launch_after(k_vertex<2>, a.vert_blocks, 256, s, a);
+    else launch_after(k_vertex<1>, a.vert_blocks, 256, s, a);
     ++n;
     if (light) join(0);
     if (a.project_g == 4) launch_after(k_cull<4>, a.total_blocks, kProjectThreads, s, a);

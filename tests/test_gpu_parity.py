@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import gorender_gb300 as gr
+from gorender_gb300 import renderer as R
 from gorender_gb300 import scenes
 from oracle import oracle
 
@@ -178,8 +179,10 @@ def test_tile_sizes_and_tiny_bins(tile):
 
 
 def test_alternating_scenes_replay_captured_frames(ctx):
-    """Frames are replayed from captured CUDA graphs keyed by their arguments;
-    five scenes in turn (more than the graphs kept) stay bit-exact."""
+    """Frames are replayed from captured CUDA graphs keyed by their arguments
+    (an asynchronous draw's graph also by its staging slot); five scenes in
+    turn, each drawn asynchronously and then synchronously (20 graphs, more
+    than are kept), stay bit-exact."""
     scs = [GOLDEN_SCENES[name]() for name in sorted(GOLDEN_SCENES)][:5]
     ups = [gr.UploadedScene(ctx, sc) for sc in scs]
     first = []
@@ -189,7 +192,8 @@ def test_alternating_scenes_replay_captured_frames(ctx):
         assert st == 0 and tpf == ref_tpf and np.array_equal(rgba, ref_rgba)
         first.append((rgba, z, tpf))
     for _ in range(3):
-        for (rgba0, z0, tpf0), up in zip(first, ups):
+        for (rgba0, z0, tpf0), sc, up in zip(first, scs, ups):
+            R.draw_async(ctx, up.items, len(sc.objects), up.params)
             rgba, z, tpf = up.render()
             assert tpf == tpf0 and np.array_equal(rgba, rgba0) and np.array_equal(z.view(np.uint32), z0.view(np.uint32))
 
