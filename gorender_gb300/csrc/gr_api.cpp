@@ -735,6 +735,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr,
       int err = 0;
       if (copy_bytes) err = launch_stage(c->d_tables, copy_src, copy_bytes, c->stream);
       if (!err) err = launch_frame(a, big_blocks, c->stream, &n, nullptr, &c->aux);
+      if (copy_bytes) ++n;  // k_stage
       const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (!err && e == cudaSuccess && g && cudaGraphInstantiate(&fg.exec, g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
@@ -755,6 +756,7 @@ int32_t launch(gr_context* c, const FrameArgs& a, void* const* events = nullptr,
   if (copy_bytes) CK((cudaError_t)launch_stage(c->d_tables, copy_src, copy_bytes, c->stream));
   int err = launch_frame(a, big_blocks, c->stream, &c->last_launches, events, &c->aux);
   if (err) return fail(GR_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
+  if (copy_bytes) ++c->last_launches;  // k_stage
   return GR_OK;
 }
 
