@@ -71,7 +71,7 @@ constexpr int kFrameGraphs = 12;
 struct FrameGraph {
   cudaGraphExec_t exec = nullptr;
   FrameArgs args{};
-  const void* copy_src = nullptr;   // the table upload captured as the graph's first node (or none)
+  const void* copy_src = nullptr;   // the staging slot k_stage reads as the graph's first kernel (or none)
   size_t copy_bytes = 0;
   int launches = 0;
   uint64_t used = 0;
@@ -486,8 +486,8 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     c->pkey_pixels = total_pixels;
   }
   // Synchronous draws stage in a slot of their own (the previous one has
-  // finished), uploaded by the frame's graph; the others rotate through the
-  // ring, each slot reused once the copy that read it has run.
+  // finished), read by the frame's graph; the others rotate through the
+  // ring, each slot reused once the copy (or the frame) that read it has run.
   const bool in_graph = upload != Upload::kCopy && !own_views && !own_items;
   const bool sync_slot = in_graph && upload == Upload::kInGraph;
   const int slot = sync_slot ? kStageSlots : (c->stage_slot + 1) % kStageSlots;
@@ -605,7 +605,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   // a graph batch keeps its own tables, so other draws cannot overwrite them
   DevView* dviews = own_views ? own_views : c->d_views;
   DevItem* ditems = own_items ? own_items : c->d_items;
-  if (in_graph) {  // both tables with one copy, the first node of the frame's graph
+  if (in_graph) {  // both tables copied by k_stage, the first kernel of the frame's graph
     const size_t bytes = live ? c->tables_off + sizeof(DevItem) * (size_t)live : sizeof(DevView) * (size_t)nviews;
     out.copy_src = hslot;
     out.copy_bytes = bytes;
