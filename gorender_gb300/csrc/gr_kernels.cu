@@ -594,14 +594,28 @@ __device__ __forceinline__ void bin_tiles_warp(const FrameArgs& a, uint32_t r, i
 }
 
 // The item owning this block: kind 0 face blocks (k_cull), 1 normal blocks
-// (k_light), 2 vertex blocks (k_vertex); the bases never decrease.
+// (k_light), 2 vertex blocks (k_vertex): the last item whose first block is
+// at most blockIdx.x (the bases never decrease; item 0's is 0).  Called by a
+// whole warp: each round probes 32 items spread over the remaining range at
+// once, so a frame of up to 32 items takes one round trip and one of 1024
+// two, where a binary search over the item table takes log2(items).
 __device__ __forceinline__ int find_item(const FrameArgs& a, int kind) {
-  int lo = 0, hi = a.num_items - 1;
+  const int lane = (int)lane_id();
+  int lo = 0, hi = a.num_items - 1;  // the answer lies in [lo, hi]
   while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    const DevItem& m = a.items[mid];
-    int base = kind == 1 ? m.light_block_base : kind == 2 ? m.vert_block_base : m.block_base;
-    if (base <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+    const int step = (hi - lo + 31) >> 5;  // probes lo + 1, lo + 1 + step, ... cover (lo, hi]
+    const int p = lo + 1 + lane * step;
+    bool ok = false;
+    if (p <= hi) {
+      const DevItem& m = a.items[p];
+      const int base = kind == 1 ? m.light_block_base : kind == 2 ? m.vert_block_base : m.block_base;
+      ok = base <= (int)blockIdx.x;
+    }
+    const unsigned got = __ballot_sync(FULL_MASK, ok);  // a prefix of the lanes
+    if (!got) break;                                     // no later item qualifies: lo
+    const int last = 31 - __clz((int)got);
+    lo += 1 + last * step;
+    hi = min(hi, lo + step - 1);
   }
   return lo;
 }
@@ -619,7 +633,10 @@ __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
   __shared__ float s_mvp[16];
   __shared__ float s_S[8];
   __shared__ int s_item;
-  if (threadIdx.x == 0) s_item = find_item(a, 2);
+  if (threadIdx.x < 32) {
+    const int item = find_item(a, 2);
+    if (threadIdx.x == 0) s_item = item;
+  }
   __syncthreads();
   const DevItem& it = a.items[s_item];
   if (threadIdx.x < 16) s_mvp[threadIdx.x] = it.mvp[threadIdx.x];
@@ -648,7 +665,10 @@ template <int G>
 __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
   __shared__ float s_world[16];
   __shared__ int s_item;
-  if (threadIdx.x == 0) s_item = find_item(a, 1);
+  if (threadIdx.x < 32) {
+    const int item = find_item(a, 1);
+    if (threadIdx.x == 0) s_item = item;
+  }
   __syncthreads();
   const DevItem& it = a.items[s_item];
   if (threadIdx.x < 16) s_world[threadIdx.x] = it.world[threadIdx.x];
@@ -680,7 +700,10 @@ __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
   __shared__ uint2 s_keep[kWarps][32 * G];  // (item, face) of the warp's kept faces
 
   const int tid = threadIdx.x;
-  if (tid == 0) s_item = find_item(a, 0);
+  if (tid < 32) {
+    const int item = find_item(a, 0);
+    if (tid == 0) s_item = item;
+  }
   __syncthreads();
   const int item = s_item;
   const DevItem& it = a.items[item];
