@@ -425,10 +425,10 @@ int32_t ensure_views(gr_context* c, int nviews, uint32_t tiles) {
   return GR_OK;
 }
 
-// How a draw's tables reach the device: a copy queued by prepare (kCopy),
-// the synchronous draws' own slot read by the frame's graph (kInGraph), or a
-// slot of the ring read by the frame's graph (kRingInGraph: the caller
-// records the slot's event after launching).
+// How a draw's tables reach the device: a k_stage queued by prepare before
+// the frame (kCopy), the synchronous draws' own slot read by the frame's
+// graph (kInGraph), or a slot of the ring read by the frame's graph
+// (kRingInGraph: the caller records the slot's event after launching).
 enum class Upload { kCopy, kInGraph, kRingInGraph };
 
 // Validates views and items, stages the view and item tables and fills the
@@ -487,7 +487,7 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
   }
   // Synchronous draws stage in a slot of their own (the previous one has
   // finished), read by the frame's graph; the others rotate through the
-  // ring, each slot reused once the copy (or the frame) that read it has run.
+  // ring, each slot reused once the k_stage (or the frame) that read it has run.
   const bool in_graph = upload != Upload::kCopy && !own_views && !own_items;
   const bool sync_slot = in_graph && upload == Upload::kInGraph;
   const int slot = sync_slot ? kStageSlots : (c->stage_slot + 1) % kStageSlots;
@@ -610,13 +610,13 @@ int32_t prepare(gr_context* c, const ViewIn* views, int nviews, const gr_draw_it
     out.copy_src = hslot;
     out.copy_bytes = bytes;
     c->h2d_bytes = (int64_t)bytes;
-  } else if (!own_views && !own_items) {  // both tables with one copy
+  } else if (!own_views && !own_items) {  // both tables with one k_stage, before the frame's graph
     const size_t bytes = live ? c->tables_off + sizeof(DevItem) * (size_t)live : sizeof(DevView) * (size_t)nviews;
-    CK(cudaMemcpyAsync(c->d_tables, hslot, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK((cudaError_t)launch_stage(c->d_tables, hslot, bytes, c->stream));
     c->h2d_bytes = (int64_t)bytes;
-  } else {
-    CK(cudaMemcpyAsync(dviews, hviews, sizeof(DevView) * nviews, cudaMemcpyHostToDevice, c->stream));
-    if (live) CK(cudaMemcpyAsync(ditems, hitems, sizeof(DevItem) * live, cudaMemcpyHostToDevice, c->stream));
+  } else {  // tables of their own (batches, the differentiable pass): one k_stage each
+    CK((cudaError_t)launch_stage(dviews, hviews, sizeof(DevView) * nviews, c->stream));
+    if (live) CK((cudaError_t)launch_stage(ditems, hitems, sizeof(DevItem) * live, c->stream));
     c->h2d_bytes = (int64_t)sizeof(DevItem) * live + (int64_t)sizeof(DevView) * nviews;
   }
   if (!in_graph) {
@@ -1218,7 +1218,7 @@ void batch_drop_graph(gr_batch* b) {
 }
 
 // Stages the batch's tables (outside any capture) and captures its frame
-// kernels plus the result copies as a CUDA graph.
+// kernels as a CUDA graph.
 int32_t batch_capture(gr_batch* b) {
   gr_context* c = b->ctx;
   batch_drop_graph(b);
@@ -1232,17 +1232,20 @@ int32_t batch_capture(gr_batch* b) {
   Prepared pr;
   int32_t st = prepare(c, b->vin.data(), nv, b->items.data(), (int)b->items.size(), true, pr, b->d_views, b->d_items);
   if (st) return st;
+  // the last raster CTA writes the counters and the per-view TPF into
+  // page-locked host memory itself: the graph ends with its kernels, no copy
+  unsigned long long* tpf_dev = nullptr;
+  CK(cudaHostGetDevicePointer((void**)&tpf_dev, c->h_view_tpf, 0));
+  pr.a.result_host = c->h_result_dev;
+  pr.a.view_tpf_out = tpf_dev;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int err = launch_frame(pr.a, kBigBlocks, c->stream, &b->launches, nullptr, &c->aux);
-  cudaError_t e2 = cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream);
-  cudaError_t e3 = cudaMemcpyAsync(c->h_view_tpf, c->view_tpf_out, sizeof(unsigned long long) * nv,
-                                   cudaMemcpyDeviceToHost, c->stream);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-  if (err || e2 || e3 || e != cudaSuccess) {
+  if (err || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
-    return fail(GR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : (cudaError_t)(err ? err : (e2 ? e2 : e3))));
+    return fail(GR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : (cudaError_t)err));
   }
   b->graph = g;
   CK(cudaGraphInstantiate(&b->exec, g, 0));
@@ -1777,10 +1780,10 @@ struct gr_diff {
   float* d_world = nullptr;
   float* bbox_partial = nullptr;        // kBBoxBlocks x 6
   unsigned* bbox_done = nullptr;
-  double* d_acc = nullptr;              // loss, light gradient x 3
   double* d_partials = nullptr;         // per-warp sums (kDiffSlots x 4), zero when idle
   float* d_gface = nullptr;             // per-face corner gradient sums (nf x 3 x 8), zero when idle
-  double* h_acc = nullptr;              // pinned
+  double* h_acc = nullptr;              // pinned: loss, light gradient x 3
+  double* h_acc_dev = nullptr;          // its device address (k_diff_sum writes the sums there)
   gr_diff_params last{};                // parameters of the last forward
   const float* last_target = nullptr;
   bool have_forward = false;
@@ -1811,8 +1814,8 @@ DiffArgs diff_args(const gr_diff* d, const gr_diff_params& p, const float* targe
   a.ids = d->ids;
   a.rec = d->rec;
   a.target = target;
-  a.loss = d->d_acc;
-  a.g_light = d->d_acc + 1;
+  a.loss = d->h_acc_dev;
+  a.g_light = d->h_acc_dev + 1;
   a.partials = d->d_partials;
   a.g_face = d->d_gface;
   return a;
@@ -1823,7 +1826,6 @@ void diff_free(gr_diff* d) {
   dev_free(d->ids); dev_free(d->z); dev_free(d->rec); dev_free(d->nhat); dev_free(d->d_world);
   dev_free(d->vh); dev_free(d->col_tab); dev_free(d->row_tab);
   dev_free(d->bbox_partial); dev_free(d->bbox_done);
-  dev_free(d->d_acc);
   dev_free(d->d_partials);
   dev_free(d->d_gface);
   if (d->h_acc) cudaFreeHost(d->h_acc);
@@ -1957,7 +1959,6 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
   if (!st) st = dev_alloc(&d->bbox_done, (size_t)1);
   if (!st && cudaMemsetAsync(d->bbox_done, 0, sizeof(unsigned), c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff counters");
-  if (!st) st = dev_alloc(&d->d_acc, (size_t)4);
   if (!st) st = dev_alloc(&d->d_partials, (size_t)kDiffSlots * 4);
   if (!st && cudaMemsetAsync(d->d_partials, 0, sizeof(double) * kDiffSlots * 4, c->stream) != cudaSuccess)
     st = fail(GR_ERR_CUDA, "diff partials");
@@ -1968,6 +1969,8 @@ int32_t gr_diff_create(gr_context* c, int32_t mesh, const float* world, int32_t 
     d->h_acc = nullptr;
     st = fail(GR_ERR_OUT_OF_MEMORY, "pinned accumulator");
   }
+  if (!st && cudaHostGetDevicePointer((void**)&d->h_acc_dev, d->h_acc, 0) != cudaSuccess)
+    st = fail(GR_ERR_CUDA, "pinned accumulator address");
   if (!st) {
     d->vin.resize(num_views);
     for (int v = 0; v < num_views; ++v)
@@ -2027,12 +2030,12 @@ int32_t gr_diff_forward(gr_diff* d, const gr_diff_params* p, const float* target
     if (st) return st;
     int e = launch_diff_bbox(p->positions, d->nv, d->d_items, nviews, d->bbox_partial, d->bbox_done, c->stream);
     if (e) return fail(GR_ERR_CUDA, "diff bbox: %s", cudaGetErrorString((cudaError_t)e));
+    // the visibility pass's counters and the loss reach page-locked host
+    // memory from the kernels themselves: no copy between or after them
+    pr.a.result_host = c->h_result_dev;
     if ((st = launch(c, pr.a))) return st;
-    CK(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemsetAsync(d->d_acc, 0, sizeof(double), c->stream));
     e = launch_diff_forward(a, d->max_side, c->stream);
     if (e) return fail(GR_ERR_CUDA, "diff forward: %s", cudaGetErrorString((cudaError_t)e));
-    CK(cudaMemcpyAsync(d->h_acc, d->d_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     int32_t err;
     const int rerun = check_result(c, *c->h_result, &err);
@@ -2066,10 +2069,8 @@ int32_t gr_diff_backward(gr_diff* d, gr_diff_grads* g) {
   CK(cudaMemsetAsync(g->positions, 0, sizeof(float) * 4 * (size_t)d->nv, c->stream));
   CK(cudaMemsetAsync(g->vertex_colors, 0, sizeof(float) * 3 * (size_t)d->nv, c->stream));
   if (a.g_tex) CK(cudaMemsetAsync(a.g_tex, 0, sizeof(float) * 4 * (size_t)d->tw * (size_t)d->th, c->stream));
-  CK(cudaMemsetAsync(d->d_acc + 1, 0, 3 * sizeof(double), c->stream));
   int e = launch_diff_backward(a, c->stream);
   if (e) return fail(GR_ERR_CUDA, "diff backward: %s", cudaGetErrorString((cudaError_t)e));
-  CK(cudaMemcpyAsync(d->h_acc + 1, d->d_acc + 1, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 3; ++k) g->light[k] = d->h_acc[1 + k];
   return GR_OK;

@@ -507,8 +507,9 @@ __global__ void __launch_bounds__(kThreads) k_diff_scatter(const DiffArgs a) {
   }
 }
 
-// Adds components [c0, c0 + n) of the per-warp slots into dst[0 .. n) and
-// returns the slots to zero.  One block of kDiffSlots threads.
+// Writes the sums of components [c0, c0 + n) of the per-warp slots to
+// dst[0 .. n) (page-locked host memory, through its device address: no copy
+// follows) and returns the slots to zero.  One block of kDiffSlots threads.
 __global__ void __launch_bounds__(kDiffSlots) k_diff_sum(const DiffArgs a, int c0, int n, double* dst) {
   __shared__ double s_w[kDiffSlots / 32];
   for (int j = 0; j < n; ++j) {
@@ -522,7 +523,7 @@ __global__ void __launch_bounds__(kDiffSlots) k_diff_sum(const DiffArgs a, int c
     if (threadIdx.x == 0) {
       double sum = 0.0;
       for (int w = 0; w < kDiffSlots / 32; ++w) sum += s_w[w];
-      dst[j] += sum;
+      dst[j] = sum;
     }
     __syncthreads();
   }

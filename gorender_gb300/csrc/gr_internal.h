@@ -340,11 +340,11 @@ struct DiffArgs {
   DiffRecord* rec;                  // per pixel
   const float* target;              // per pixel RGBA
   float* image;                     // per pixel RGBA (may be null)
-  double* loss;                     // one value, accumulated
+  double* loss;                     // one value (page-locked host memory, its device address)
   float* g_pos;                     // nv x 4 (w left 0)
   float* g_vcol;                    // nv x 3
   float* g_tex;                     // th x tw x 4
-  double* g_light;                  // 3, accumulated
+  double* g_light;                  // 3 (page-locked host memory, its device address)
   double* partials;                 // kDiffSlots x {loss, light x, y, z}: per-warp sums, zero when idle
   float* g_face;                    // nf x 3 corners x {colour r, g, b, position x, y, z, 0, 0}: the
                                     // backward's per-face sums before k_diff_scatter (zero when idle),
@@ -369,8 +369,8 @@ struct AuxStream {
 int launch_frame(const FrameArgs& a, int big_blocks, void* stream, int* launches, void* const* events,
                  const AuxStream* aux = nullptr);
 
-// Copies bytes (rounded up to 16; both buffers are 256-byte strided) from a
-// page-locked staging slot to the device tables with one small kernel.
+// Copies bytes from a page-locked staging slot (its device address) to
+// device memory with one small kernel (16-byte aligned buffers).
 int launch_stage(void* dst, const void* src, size_t bytes, void* stream);
 
 // Persistent raster grid: SMs x resident CTAs of k_raster<TS> x waves.

@@ -2132,15 +2132,25 @@ __device__ __forceinline__ void clear_quad(const FrameArgs& a, uint2 e, uint32_t
 // into the device tables, as the first kernel of the frame, so the frame's
 // kernels follow a kernel on their stream instead of a copy-engine transfer.
 // One 16-byte word a thread, so the reads that cross to host memory are all
-// in flight at once (a 64-item table is 23.5 KB).
-__global__ void __launch_bounds__(128) k_stage(uint4* __restrict__ dst, const uint4* __restrict__ src, uint32_t n16) {
+// in flight at once (a 64-item table is 23.5 KB); the thread after the last
+// whole word copies the remaining bytes one by one.
+__global__ void __launch_bounds__(128) k_stage(uint4* __restrict__ dst, const uint4* __restrict__ src, uint32_t n16,
+                                               uint32_t tail) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n16) dst[i] = __ldcv(src + i);
+  if (i < n16) {
+    dst[i] = __ldcv(src + i);
+  } else if (i == n16) {
+    const unsigned char* s = reinterpret_cast<const unsigned char*>(src + n16);
+    unsigned char* d = reinterpret_cast<unsigned char*>(dst + n16);
+    for (uint32_t k = 0; k < tail; ++k) d[k] = __ldcv(s + k);
+  }
 }
 
 int launch_stage(void* dst, const void* src, size_t bytes, void* stream) {
-  const uint32_t n16 = (uint32_t)((bytes + 15) / 16);
-  k_stage<<<(n16 + 127) / 128, 128, 0, (cudaStream_t)stream>>>((uint4*)dst, (const uint4*)src, n16);
+  const uint32_t n16 = (uint32_t)(bytes / 16), tail = (uint32_t)(bytes % 16);
+  const uint32_t threads = n16 + (tail ? 1u : 0u);
+  if (!threads) return 0;
+  k_stage<<<(threads + 127) / 128, 128, 0, (cudaStream_t)stream>>>((uint4*)dst, (const uint4*)src, n16, tail);
   return (int)cudaGetLastError();
 }
 
