@@ -2135,7 +2135,8 @@ struct gr_presenter {
   cudaStream_t copy = nullptr;
   uint32_t* dev[2] = {nullptr, nullptr};
   uint8_t* host[2] = {nullptr, nullptr};      // pinned
-  DevResult* res[2] = {nullptr, nullptr};     // pinned: each frame's counters
+  DevResult* res[2] = {nullptr, nullptr};     // pinned: each frame's counters (and the raster's done word)
+  DevResult* res_dev[2] = {nullptr, nullptr}; // their device addresses: the last raster CTA writes there
   cudaEvent_t rendered[2] = {}, copied[2] = {};
   std::vector<gr_draw_item> items[2];
   bool queued[2] = {false, false};            // rendered + copy queued, not yet returned
@@ -2173,8 +2174,8 @@ int32_t presenter_enqueue(gr_presenter* p, int b) {
   int32_t st = prepare(c, &v, 1, p->items[b].data(), (int32_t)p->items[b].size(), false, pr, nullptr, nullptr,
                        Upload::kRingInGraph);
   if (st) return st;
+  pr.a.result_host = p->res_dev[b];  // the counters without a copy on the render stream
   if ((st = launch(c, pr.a, nullptr, pr.copy_src, pr.copy_bytes)) || (st = record_ring_slot(c, pr))) return st;
-  CK(cudaMemcpyAsync(p->res[b], c->d_result, sizeof(DevResult), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaEventRecord(p->rendered[b], c->stream));
   CK(cudaStreamWaitEvent(p->copy, p->rendered[b], 0));
   CK(cudaMemcpyAsync(p->host[b], p->dev[b], (size_t)r->width * r->height * 4, cudaMemcpyDeviceToHost, p->copy));
@@ -2222,7 +2223,8 @@ int32_t gr_presenter_create(gr_renderer* r, gr_presenter** out) {
   for (int b = 0; b < 2 && !st; ++b) {
     if ((st = dev_alloc(&p->dev[b], px))) break;
     e = cudaMallocHost((void**)&p->host[b], px * 4);
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->res[b], sizeof(DevResult));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->res[b], 2 * sizeof(DevResult));
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&p->res_dev[b], p->res[b], 0);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->rendered[b], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->copied[b], cudaEventDisableTiming);
     if (e != cudaSuccess) st = fail(GR_ERR_CUDA, "presenter buffers: %s", cudaGetErrorString(e));
