@@ -721,13 +721,29 @@ __global__ void __launch_bounds__(kProjectThreads) k_cull(const FrameArgs a) {
   uint2* keep_list = s_keep[warp];
   int nkeep = 0;
   const int fgroup = ((int)blockIdx.x - it.block_base) * (kProjectThreads * G) + warp * (32 * G);
+  const int nf = it.nf;
+  const int* vidx = it.vidx;
+  // A face's vertex indices are loaded one face ahead (G > 1), so that the
+  // next load from memory overlaps this face's corner gathers and tests.
+  int n0 = 0, n1 = 0, n2 = 0;
+  if (fgroup + (int)lane < nf) {
+    const int f = fgroup + (int)lane;
+    n0 = __ldg(vidx + 3 * f);
+    n1 = __ldg(vidx + 3 * f + 1);
+    n2 = __ldg(vidx + 3 * f + 2);
+  }
 #pragma unroll
   for (int k = 0; k < G; ++k) {
     const int f = fgroup + k * 32 + (int)lane;
+    const int i0 = n0, i1 = n1, i2 = n2;
+    if (k + 1 < G && f + 32 < nf) {
+      n0 = __ldg(vidx + 3 * (f + 32));
+      n1 = __ldg(vidx + 3 * (f + 32) + 1);
+      n2 = __ldg(vidx + 3 * (f + 32) + 2);
+    }
     bool draw = false;
     bool general = false;  // this face needs the general clipper (k_clip)
-    if (f < it.nf) {
-      const int i0 = __ldg(it.vidx + 3 * f), i1 = __ldg(it.vidx + 3 * f + 1), i2 = __ldg(it.vidx + 3 * f + 2);
+    if (f < nf) {
       const float4 c0 = __ldg(a.vclip + it.vert_base + i0), c1 = __ldg(a.vclip + it.vert_base + i1),
                    c2 = __ldg(a.vclip + it.vert_base + i2);
       const V4 v0{c0.x, c0.y, c0.z, c0.w}, v1{c1.x, c1.y, c1.z, c1.w}, v2{c2.x, c2.y, c2.z, c2.w};
