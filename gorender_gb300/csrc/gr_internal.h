@@ -29,10 +29,11 @@ constexpr int kDefaultSliceCost = 8192;       // raster cost per slice before a 
 constexpr int kEntryCost = 32;                // raster cost of a bin entry covering <= kSmallBox pixels
 constexpr int kSmallBox = 64;                 // larger tile-clipped boxes add their area to the tile's cost
 // k_setup: resident CTAs an SM by the frame's face count (its k_cull lane
-// count): 2 (up to 128 registers a thread, no spills) below 1 M faces; 3 (up to
-// 85 registers, a few bytes spilled) from 1 M faces on, where more warps hide
-// more of the gathers (same-box A/B: the 256-view batch 40 us faster, the
-// 5 M-face frame 3 us; the 200k-face frame 1.5 us slower with 3)
+// count): 2 (at most 104 registers a thread, no spills, room for a k_clip CTA
+// beside them) below 1 M faces; 3 (at most 80 registers, 64 bytes spilled)
+// from 1 M faces on, where more warps hide more of the gathers (same-box A/B:
+// the 256-view batch 40 us faster, the 5 M-face frame 3 us; the 200k-face
+// frame 1.5 us slower with 3)
 __host__ __device__ constexpr int setup_ctas_per_sm(int project_g) { return project_g >= 2 ? 3 : 2; }
 // k_setup grid (grid-stride over the kept faces)
 __host__ __device__ constexpr int setup_blocks_max(int project_g) { return setup_ctas_per_sm(project_g) * 152; }
