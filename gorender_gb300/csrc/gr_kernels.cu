@@ -87,6 +87,14 @@ __device__ __forceinline__ V4 ld4(const float* p) {
   return V4{q.x, q.y, q.z, q.w};
 }
 
+// The same for data read once a frame (vertex positions and normals in
+// k_vertex and k_light): evict-first, so the per-vertex results, indices and
+// records that later kernels gather stay in L2 instead.
+__device__ __forceinline__ V4 ld4_stream(const float* p) {
+  float4 q = __ldcs(reinterpret_cast<const float4*>(p));
+  return V4{q.x, q.y, q.z, q.w};
+}
+
 // Frustum planes (clipping.go:93-129) with zNear = 0, zFar = 50 (renderer.go:121).
 __constant__ float c_plane_p[6][4] = {{-1, 0, 0, 1}, {1, 0, 0, 1}, {0, -1, 0, 1},
                                       {0, 1, 0, 1},  {0, 0, 0, 1}, {0, 0, 50, 1}};
@@ -647,7 +655,7 @@ __global__ void __launch_bounds__(256) k_vertex(const FrameArgs a) {
   for (int k = 0; k < G; ++k) {
     const int v = v0 + k * 256;
     if (v < it.nv) {
-      const V4 c = mat_vec(s_mvp, ld4(it.pos + 4 * (size_t)v));
+      const V4 c = mat_vec(s_mvp, ld4_stream(it.pos + 4 * (size_t)v));
       a.vclip[it.vert_base + v] = make_float4(c.x, c.y, c.z, c.w);
       const float2 sc = screen_of(c, s_S);
       a.vscr[it.vert_base + v] = make_float4(sc.x, sc.y, c.w, 0.0f);  // W beside x, y: one gather in k_setup
@@ -678,7 +686,8 @@ __global__ void __launch_bounds__(256) k_light(const FrameArgs a) {
 #pragma unroll
   for (int k = 0; k < G; ++k) {
     const int n = n0 + k * 256;
-    if (n < it.nn) a.vlight[it.light_base + n] = light_of(s_world, ld4(it.vnrm + 4 * (size_t)n), a.views[it.view].L);
+    if (n < it.nn)
+      a.vlight[it.light_base + n] = light_of(s_world, ld4_stream(it.vnrm + 4 * (size_t)n), a.views[it.view].L);
   }
 }
 
